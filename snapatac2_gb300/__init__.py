@@ -1,0 +1,39 @@
+"""GB300-native implementation of SnapATAC2's cell-embedding path.
+
+Drop-in API (same names, keywords, defaults and output slots as
+``snapatac2.pp`` / ``snapatac2.tl``):
+
+* ``pp.add_tile_matrix``  -- fragments -> cell x 500 bp tile counts (GPU)
+* ``pp.select_features``  -- most accessible tiles (host NumPy)
+* ``tl.spectral``         -- matrix-free cosine spectral embedding (GPU)
+* ``pp.knn``              -- exact Euclidean kNN graph (GPU)
+
+All compute goes through ``libsnapgb300.so`` (C ABI in ``include/snapgb300.h``).
+"""
+from . import genome  # noqa: F401
+from ._anndata import AnnData, is_anndata  # noqa: F401
+
+
+class _Namespace:
+    def __init__(self, **kw):
+        self.__dict__.update(kw)
+
+
+def __getattr__(name):
+    # lazy namespaces so that importing the package needs neither a GPU nor torch.cuda
+    if name == "pp":
+        from . import preprocessing as _p
+        from . import _knn_api as _k
+        ns = _Namespace(add_tile_matrix=_p.add_tile_matrix, select_features=_p.select_features,
+                        knn=_k.knn, fragments_to_anndata=_p.fragments_to_anndata)
+        globals()["pp"] = ns
+        return ns
+    if name == "tl":
+        from . import tools as _t
+        ns = _Namespace(spectral=_t.spectral)
+        globals()["tl"] = ns
+        return ns
+    raise AttributeError(name)
+
+
+__version__ = "0.1.0"

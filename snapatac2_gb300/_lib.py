@@ -1,0 +1,132 @@
+"""Loader of ``libsnapgb300.so``, the C ABI declared in ``include/snapgb300.h``.
+
+The library is built in-tree by ``snapatac2_gb300.build.build_library`` (nvcc,
+``-gencode arch=compute_103a,code=sm_103a``).  There is no CPU fallback: every
+compute entry point of this package goes through this library and raises
+``RuntimeError`` when it is missing or when no CUDA device is present.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+import torch
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libsnapgb300.so")
+
+SG_OK = 0
+SG_ERR_ARG = 1
+SG_ERR_RANGE = 2
+SG_ERR_CAP = 3
+SG_ERR_CUDA = 4
+SG_ERR_NUMERIC = 5
+
+_P = ctypes.c_void_p
+_I64 = ctypes.c_int64
+_I32 = ctypes.c_int
+_U32 = ctypes.c_uint32
+_F64 = ctypes.c_double
+
+# name -> (restype, argtypes); must match include/snapgb300.h
+SIGNATURES: dict[str, tuple] = {
+    "sg_version": (_I32, []),
+    "sg_status_string": (ctypes.c_char_p, [_I32]),
+    "sg_scan_scratch_bytes": (_I64, [_I64]),
+    "sg_tile_scratch_bytes": (_I64, [_I64]),
+    "sg_tile_plan": (_I32, [_P, _I64, _I64, _P, _P, _P, _P, _P, _I32, _U32, _I32, _I64, _I64, _P, _P,
+                            _P, _P, _P]),
+    "sg_tile_run": (_I32, [_P, _I64, _I64, _P, _P, _P, _P, _P, _I32, _U32, _I32, _I64, _I64, _P, _P,
+                           _I64, _P, _P, _P, _P, _P]),
+    "sg_tile_emit": (_I32, [_I64, _P, _P, _I64, _P, _P, _P, _I64, _P, _P]),
+}
+
+_lock = threading.Lock()
+_lib: ctypes.CDLL | None = None
+
+
+class SnapGB300Error(RuntimeError):
+    """A status code other than SG_OK returned by the C ABI."""
+
+    def __init__(self, code: int, what: str):
+        self.code = code
+        super().__init__(f"{what}: {status_string(code)} (status {code})")
+
+
+def load(path: str | None = None) -> ctypes.CDLL:
+    """Load the shared library (no CUDA device needed to load it)."""
+    global _lib
+    with _lock:
+        if _lib is not None and path is None:
+            return _lib
+        p = path or LIB_PATH
+        if not os.path.exists(p):
+            raise RuntimeError(
+                f"{p} is missing: build the CUDA library first "
+                "(python -c 'import __graft_entry__ as g; g.build()')")
+        lib = ctypes.CDLL(p)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        if path is None:
+            _lib = lib
+        return lib
+
+
+def status_string(code: int) -> str:
+    try:
+        return load().sg_status_string(int(code)).decode()
+    except Exception:  # noqa: BLE001 - used inside error paths
+        return "unknown"
+
+
+def lib() -> ctypes.CDLL:
+    """The library, after checking that a CUDA device is usable."""
+    if not torch.cuda.is_available():
+        raise RuntimeError("snapatac2_gb300 needs a CUDA GPU (sm_103a); none is available")
+    return load()
+
+
+def check(code: int, what: str) -> None:
+    if code != SG_OK:
+        raise SnapGB300Error(int(code), what)
+
+
+def ptr(t: torch.Tensor | None) -> int | None:
+    if t is None:
+        return None
+    if not t.is_cuda:
+        raise ValueError("expected a CUDA tensor")
+    return t.data_ptr()
+
+
+def stream_handle(device: torch.device | None = None) -> int:
+    return torch.cuda.current_stream(device).cuda_stream
+
+
+class DeviceStatus:
+    """Device-side status word + lowest offending index (see the C header)."""
+
+    def __init__(self, device):
+        self.buf = torch.zeros(2, dtype=torch.int64, device=device)
+        self.buf[1] = -1  # 0xffff... as uint64: no offending entry yet
+
+    @property
+    def status_ptr(self) -> int:
+        return self.buf.data_ptr()
+
+    @property
+    def bad_ptr(self) -> int:
+        return self.buf.data_ptr() + 8
+
+    def raise_if_error(self, what: str, index_name: str = "entry") -> None:
+        v = self.buf.cpu().tolist()
+        st = int(v[0]) & 0xFFFFFFFF
+        if st != SG_OK:
+            bad = v[1] & 0xFFFFFFFFFFFFFFFF
+            extra = "" if bad == 0xFFFFFFFFFFFFFFFF else f" (first offending {index_name}: {bad})"
+            err = SnapGB300Error(st, what + extra)
+            err.bad_index = None if bad == 0xFFFFFFFFFFFFFFFF else bad
+            raise err

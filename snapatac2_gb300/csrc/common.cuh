@@ -1,0 +1,194 @@
+// Shared device helpers for the snapgb300 kernels (sm_103a).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "snapgb300.h"
+
+#define SG_CHECK_LAUNCH()                                   \
+  do {                                                      \
+    cudaError_t e__ = cudaGetLastError();                   \
+    if (e__ != cudaSuccess) return SG_ERR_CUDA;             \
+  } while (0)
+
+namespace sg {
+
+constexpr int kWarp = 32;
+
+__device__ __forceinline__ unsigned lanemask_lt() {
+  unsigned m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+// Record the first error: status word goes from 0 to `code`, and the lowest
+// offending entry index is kept.
+__device__ __forceinline__ void report_error(int* status, unsigned long long* bad, int code,
+                                             unsigned long long entry) {
+  atomicCAS(status, 0, code);
+  if (bad) atomicMin(bad, entry);
+}
+
+// Exclusive scan of one int per thread across the block; returns the prefix
+// and writes the block total.  `ws` needs blockDim.x/32 + 1 ints of shared
+// memory.  All threads must call it.
+template <int BLOCK>
+__device__ __forceinline__ int block_exscan(int v, int* ws, int& total) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  int x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) ws[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    constexpr int NW = BLOCK / 32;
+    int s = lane < NW ? ws[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, s, o);
+      if (lane >= o) s += y;
+    }
+    if (lane < NW) ws[lane] = s;  // inclusive per-warp totals
+  }
+  __syncthreads();
+  int warp_off = wid ? ws[wid - 1] : 0;
+  total = ws[BLOCK / 32 - 1];
+  __syncthreads();
+  return warp_off + x - v;
+}
+
+template <int BLOCK>
+__device__ __forceinline__ long long block_sum_ll(long long v, long long* ws) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  if (lane == 0) ws[wid] = v;
+  __syncthreads();
+  long long t = 0;
+  if (threadIdx.x == 0) {
+    for (int w = 0; w < BLOCK / 32; ++w) t += ws[w];
+    ws[0] = t;
+  }
+  __syncthreads();
+  t = ws[0];
+  __syncthreads();
+  return t;
+}
+
+template <int BLOCK>
+__device__ __forceinline__ unsigned block_min_u32(unsigned v, unsigned* ws) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = min(v, __shfl_down_sync(0xffffffffu, v, o));
+  if (lane == 0) ws[wid] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned t = ws[0];
+    for (int w = 1; w < BLOCK / 32; ++w) t = min(t, ws[w]);
+    ws[0] = t;
+  }
+  __syncthreads();
+  unsigned r = ws[0];
+  __syncthreads();
+  return r;
+}
+
+template <int BLOCK>
+__device__ __forceinline__ unsigned block_max_u32(unsigned v, unsigned* ws) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_down_sync(0xffffffffu, v, o));
+  if (lane == 0) ws[wid] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned t = ws[0];
+    for (int w = 1; w < BLOCK / 32; ++w) t = max(t, ws[w]);
+    ws[0] = t;
+  }
+  __syncthreads();
+  unsigned r = ws[0];
+  __syncthreads();
+  return r;
+}
+
+// Shared-memory workspace of the CTA radix sort.
+template <int BLOCK>
+struct SortSmem {
+  unsigned offs[256];              // running digit offsets
+  unsigned tot[256];               // digit counts of the current tile
+  unsigned wcnt[BLOCK / 32][256];  // per-warp digit counts -> per-warp offsets
+  unsigned ws[BLOCK / 32 + 1];
+};
+
+// Stable LSD radix sort (8-bit digits) of n keys by (key - kmin), done by one
+// CTA.  `a` holds the input; `b` is scratch of the same size.  Both may live
+// in shared or global memory (generic addressing).  Returns the buffer that
+// holds the sorted keys.  All threads of the block must call it.
+template <int BLOCK>
+__device__ uint32_t* cta_radix_sort(uint32_t* a, uint32_t* b, int n, uint32_t kmin, int nbits,
+                                    SortSmem<BLOCK>& sm) {
+  static_assert(BLOCK >= 256 && BLOCK % 32 == 0, "BLOCK must cover the 256 digits");
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  constexpr int NW = BLOCK / 32;
+  for (int shift = 0; shift < nbits; shift += 8) {
+    if (tid < 256) {
+      sm.offs[tid] = 0;
+      for (int w = 0; w < NW; ++w) sm.wcnt[w][tid] = 0;
+    }
+    __syncthreads();
+    for (int i = tid; i < n; i += BLOCK) atomicAdd(&sm.offs[((a[i] - kmin) >> shift) & 255u], 1u);
+    __syncthreads();
+    if (wid == 0) {  // exclusive scan of the 256 digit counts, 8 per lane
+      unsigned v[8], s = 0;
+#pragma unroll
+      for (int j = 0; j < 8; ++j) { v[j] = sm.offs[lane * 8 + j]; s += v[j]; }
+      unsigned x = s;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        unsigned y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+      }
+      unsigned run = x - s;
+#pragma unroll
+      for (int j = 0; j < 8; ++j) { sm.offs[lane * 8 + j] = run; run += v[j]; }
+    }
+    __syncthreads();
+    // stable scatter, one tile of BLOCK keys at a time in input order
+    for (int base = 0; base < n; base += BLOCK) {
+      const int i = base + tid;
+      const bool valid = i < n;
+      const uint32_t key = valid ? a[i] : 0u;
+      const unsigned d = valid ? (((key - kmin) >> shift) & 255u) : 256u;
+      const unsigned peers = __match_any_sync(0xffffffffu, d);
+      const unsigned rank = __popc(peers & lanemask_lt());
+      if (valid && lane == __ffs(peers) - 1) sm.wcnt[wid][d] = __popc(peers);
+      __syncthreads();
+      if (tid < 256) {  // exclusive prefix over warps for digit tid
+        unsigned run = 0;
+        for (int w = 0; w < NW; ++w) {
+          unsigned c = sm.wcnt[w][tid];
+          sm.wcnt[w][tid] = run;
+          run += c;
+        }
+        sm.tot[tid] = run;
+      }
+      __syncthreads();
+      if (valid) b[sm.offs[d] + sm.wcnt[wid][d] + rank] = key;
+      __syncthreads();
+      if (tid < 256) {
+        sm.offs[tid] += sm.tot[tid];
+        for (int w = 0; w < NW; ++w) sm.wcnt[w][tid] = 0;
+      }
+      __syncthreads();
+    }
+    uint32_t* t = a;
+    a = b;
+    b = t;
+  }
+  return a;
+}
+
+}  // namespace sg

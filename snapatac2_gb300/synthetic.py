@@ -1,0 +1,204 @@
+"""Seeded synthetic inputs for the cell-embedding path.
+
+No public dataset ships with the reference (its fixtures are git-LFS stubs and
+``snap.datasets`` downloads over HTTP), so these generators stand in for real
+scATAC-seq data with the shapes and value distributions of the workloads:
+
+* a 3.1 Gb genome in 24 chromosomes (``chr1`` .. ``chr22``, ``chrX``, ``chrY``);
+* per-cell fragment counts ~ LogNormal(ln median, sigma);
+* cells drawn from ``n_clusters`` clusters, each with its own enriched set of
+  500 bp genome tiles weighted by Zipf(a); a fragment lands in the cluster's
+  enriched set with probability ``p_enriched`` and uniformly elsewhere;
+* fragment lengths ~ Geometric with mean 200 bp, clipped so that a fragment
+  never runs past the end of its chromosome (the reference panics otherwise,
+  ``snapatac2-core/src/genome.rs:397-399``).
+
+The fragment output uses the reference's ``obsm['fragment_paired']`` encoding
+(``snapatac2-core/src/preprocessing/import.rs:22-30,161-210``): one row per
+cell, column = global 0-based base index of the fragment start, value =
+fragment length; each row sorted by (start, length).
+
+``binary_csr`` draws the cell-by-feature matrices of the large workloads
+directly: binary CSR over ``n_features`` columns with the same cluster/Zipf
+model, int64 ``indptr`` and int32 sorted, de-duplicated column indices.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+
+import numpy as np
+
+
+def make_genome(total: int = 3_100_000_000, n_chrom: int = 24) -> list[tuple[str, int]]:
+    """Chromosome names and sizes summing to ``total``.
+
+    Sizes decrease linearly from chr1 to chrX; chrY is a quarter of chr1.
+    """
+    names = [f"chr{i}" for i in range(1, n_chrom - 1)] + ["chrX", "chrY"][: max(0, min(2, n_chrom))]
+    names = names[:n_chrom]
+    w = np.array([1.0 - 0.035 * i for i in range(n_chrom)], dtype=np.float64)
+    if n_chrom >= 2:
+        w[-1] = 0.25
+    sizes = np.floor(w / w.sum() * total).astype(np.int64)
+    sizes[0] += total - int(sizes.sum())
+    return [(n, int(s)) for n, s in zip(names, sizes)]
+
+
+@dataclass
+class FragmentMatrix:
+    """Paired-end fragments in the ``fragment_paired`` encoding."""
+
+    indptr: np.ndarray   # int64 [n_cells + 1]
+    pos: np.ndarray      # uint64 [F]  global 0-based base index of the start
+    length: np.ndarray   # uint32 [F]  fragment length in bp
+    clusters: np.ndarray  # int32 [n_cells] generating cluster of each cell
+
+    @property
+    def n_cells(self) -> int:
+        return int(self.indptr.shape[0] - 1)
+
+    @property
+    def n_fragments(self) -> int:
+        return int(self.pos.shape[0])
+
+
+def _zipf_cdf(n: int, a: float) -> np.ndarray:
+    w = np.arange(1, n + 1, dtype=np.float64) ** (-a)
+    c = np.cumsum(w)
+    return c / c[-1]
+
+
+def make_fragments(
+    n_cells: int,
+    genome: list[tuple[str, int]] | None = None,
+    *,
+    n_clusters: int = 8,
+    enriched_bins: int = 50_000,
+    zipf_a: float = 1.1,
+    p_enriched: float = 0.7,
+    median_frags: float = 10_000.0,
+    sigma: float = 0.6,
+    mean_len: float = 200.0,
+    bin_size: int = 500,
+    seed: int = 0,
+) -> FragmentMatrix:
+    """Draw ``n_cells`` cells of paired-end fragments (see module docstring)."""
+    if genome is None:
+        genome = make_genome()
+    rng = np.random.Generator(np.random.PCG64(seed))
+    sizes = np.array([s for _, s in genome], dtype=np.int64)
+    base_end = np.cumsum(sizes)
+    base_start = base_end - sizes
+    gsize = int(base_end[-1])
+    nb = -(-sizes // bin_size)
+    bin_end = np.cumsum(nb)
+    bin_start = bin_end - nb
+    total_bins = int(bin_end[-1])
+    n_enr = min(enriched_bins, total_bins)
+
+    counts = np.maximum(1, np.rint(rng.lognormal(np.log(median_frags), sigma, n_cells))).astype(np.int64)
+    clusters = rng.integers(0, n_clusters, n_cells).astype(np.int32)
+    enr = np.stack([rng.choice(total_bins, n_enr, replace=False) for _ in range(n_clusters)])
+    cdf = _zipf_cdf(n_enr, zipf_a)
+
+    F = int(counts.sum())
+    cell = np.repeat(np.arange(n_cells, dtype=np.int64), counts)
+    length = rng.geometric(1.0 / mean_len, F).astype(np.int64)
+    is_enr = rng.random(F) < p_enriched
+    gpos = np.empty(F, dtype=np.int64)
+    # enriched draws: a Zipf-ranked tile of the cell's cluster, uniform inside it
+    ne = int(is_enr.sum())
+    rank = np.searchsorted(cdf, rng.random(ne), side="right").clip(0, n_enr - 1)
+    gbin = enr[clusters[cell[is_enr]], rank]
+    chrom = np.searchsorted(bin_end, gbin, side="right")
+    off = (gbin - bin_start[chrom]) * bin_size + rng.integers(0, bin_size, ne)
+    off = np.minimum(off, sizes[chrom] - 1)
+    gpos[is_enr] = base_start[chrom] + off
+    # background draws: uniform over the genome
+    nbk = F - ne
+    gpos[~is_enr] = rng.integers(0, gsize, nbk)
+    # clip so that start + length <= chromosome length
+    chrom = np.searchsorted(base_end, gpos, side="right")
+    off = gpos - base_start[chrom]
+    csz = sizes[chrom]
+    length = np.minimum(length, csz)
+    off = np.minimum(off, csz - length)
+    gpos = base_start[chrom] + off
+
+    # sort each row by (start, length)
+    order = np.argsort(length, kind="stable")
+    key = (cell[order] << np.int64(34)) | gpos[order]
+    order = order[np.argsort(key, kind="stable")]
+    indptr = np.zeros(n_cells + 1, dtype=np.int64)
+    np.cumsum(counts, out=indptr[1:])
+    return FragmentMatrix(
+        indptr=indptr,
+        pos=gpos[order].astype(np.uint64),
+        length=length[order].astype(np.uint32),
+        clusters=clusters,
+    )
+
+
+@dataclass
+class BinaryCSR:
+    """Binary (implicit 1.0) cell-by-feature CSR matrix."""
+
+    indptr: np.ndarray   # int64 [n + 1]
+    indices: np.ndarray  # int32 [nnz], sorted and unique within each row
+    n_cols: int
+    clusters: np.ndarray  # int32 [n]
+
+    @property
+    def shape(self) -> tuple[int, int]:
+        return (int(self.indptr.shape[0] - 1), int(self.n_cols))
+
+    @property
+    def nnz(self) -> int:
+        return int(self.indices.shape[0])
+
+
+def binary_csr(
+    n_cells: int,
+    n_features: int = 500_000,
+    *,
+    nnz_per_cell: float = 4_000.0,
+    sigma: float = 0.3,
+    n_clusters: int = 8,
+    enriched: int = 50_000,
+    zipf_a: float = 1.1,
+    p_enriched: float = 0.7,
+    seed: int = 0,
+    chunk_cells: int = 20_000,
+) -> BinaryCSR:
+    """Binary CSR with ~``nnz_per_cell`` distinct features per row.
+
+    Per row, ``d`` ~ LogNormal(ln(nnz_per_cell), sigma) features are drawn
+    (``p_enriched`` of them Zipf-ranked from the cluster's enriched set, the
+    rest uniform) and de-duplicated.
+    """
+    rng = np.random.Generator(np.random.PCG64(seed))
+    n_enr = min(enriched, n_features)
+    draws = np.maximum(1, np.rint(rng.lognormal(np.log(nnz_per_cell), sigma, n_cells))).astype(np.int64)
+    draws = np.minimum(draws, n_features)
+    clusters = rng.integers(0, n_clusters, n_cells).astype(np.int32)
+    enr = np.stack([rng.choice(n_features, n_enr, replace=False) for _ in range(n_clusters)]).astype(np.int64)
+    cdf = _zipf_cdf(n_enr, zipf_a)
+    rows_idx = []
+    row_nnz = np.zeros(n_cells, dtype=np.int64)
+    for c0 in range(0, n_cells, chunk_cells):
+        c1 = min(n_cells, c0 + chunk_cells)
+        d = draws[c0:c1]
+        D = int(d.sum())
+        cell = np.repeat(np.arange(c0, c1, dtype=np.int64), d)
+        is_enr = rng.random(D) < p_enriched
+        col = rng.integers(0, n_features, D)
+        ne = int(is_enr.sum())
+        rank = np.searchsorted(cdf, rng.random(ne), side="right").clip(0, n_enr - 1)
+        col[is_enr] = enr[clusters[cell[is_enr]], rank]
+        key = np.unique((cell << np.int64(32)) | col)
+        r = key >> np.int64(32)
+        rows_idx.append((key & np.int64(0xFFFFFFFF)).astype(np.int32))
+        row_nnz[c0:c1] = np.bincount(r - c0, minlength=c1 - c0)
+    indptr = np.zeros(n_cells + 1, dtype=np.int64)
+    np.cumsum(row_nnz, out=indptr[1:])
+    return BinaryCSR(indptr=indptr, indices=np.concatenate(rows_idx), n_cols=n_features, clusters=clusters)
