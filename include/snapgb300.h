@@ -101,6 +101,110 @@ int sg_tile_emit(int64_t n_cells, const int64_t* key_ptr, const void* scratch,
                  int64_t scratch_bytes, const int64_t* out_indptr, int32_t* out_idx,
                  uint32_t* out_cnt, int64_t cap, int* status, void* stream);
 
+
+/* ------------------------------------------------------------------------ */
+/* Spectral embedding (matrix-free cosine) -- replaces spectral_embedding    */
+/*   (snapatac2-python/src/embedding.rs:24-59): column slice + idf +         */
+/*   normalize + spectral_mf degree (embedding.rs:133-152,269-286,315-326)   */
+/*   and the SciPy ARPACK eigsh call on X̂X̂ᵀ - D⁻¹ (embedding.rs:155-188).    */
+/*                                                                           */
+/* Matrices are CSR with int64 row pointers and int32 column indices, rows   */
+/* sorted and unique.  values == NULL means the implicit 1.0 pattern.        */
+/* dtype: 0 = float32 (mixed precision), 1 = float64.                        */
+/* ------------------------------------------------------------------------ */
+
+/* Keep the entries whose column maps to colmap[col] >= 0, renumbered to     */
+/* colmap[col] (X[:, selected_features], embedding.rs:36-41).  out_indices /  */
+/* out_values need capacity nnz(input); out_indptr[n] = kept nnz.            */
+int sg_csr_select_cols(int64_t n, const int64_t* indptr, const int32_t* indices, const float* values,
+                       const int32_t* colmap, int64_t* out_indptr, int32_t* out_indices, float* out_values,
+                       void* scan_scratch, void* stream);
+
+/* Number of row blocks used by sg_csr_transpose (work = nblk * m int32).   */
+int sg_transpose_blocks(void);
+
+/* Deterministic CSR -> CSC transpose (rows ascending in every column).     */
+/* colptr[m+1] (int64), rowidx[nnz], cvalues[nnz] (NULL if values NULL).     */
+/* Unsorted / duplicate / out-of-range column indices -> status SG_ERR_ARG.  */
+int sg_csr_transpose(int64_t n, int64_t m, const int64_t* indptr, const int32_t* indices,
+                     const float* values, int nblk, int32_t* work, int64_t* colptr, int32_t* rowidx,
+                     float* cvalues, void* scan_scratch, int* status, void* stream);
+
+/* Operator set-up in FP64: w = idf (or a copy of feature_weights when not  */
+/* NULL), w2 = w², rinv = 1/||(XW)_i||, colsum = 1ᵀXn, dinv = 1/(d - 1),    */
+/* a = rinv * sqrt(dinv); float copies w2_32/a32/dinv32 may be NULL.        */
+/* minmax: 2 uint64 of scratch.  A zero row or a non-positive d - 1 sets    */
+/* status SG_ERR_NUMERIC with the row in bad (the reference yields NaN).     */
+int sg_spectral_prepare(int64_t n, int64_t m, const int64_t* indptr, const int32_t* indices,
+                        const float* values, const int64_t* colptr, const int32_t* rowidx,
+                        const float* cvalues, const double* feature_weights, double* w, double* w2,
+                        float* w2_32, double* rinv, double* colsum, double* a, double* dinv, float* a32,
+                        float* dinv32, unsigned long long* minmax, int* status, unsigned long long* bad,
+                        void* stream);
+
+/* SpMM over a block of `block` (4, 8, 16, 32) dense columns:               */
+/*   out[r,:] = scale[r] * sum_{e in row r} val_e * in[col_e,:]              */
+/*              - dshift[r] * y[r,:]            (when dshift != NULL)       */
+/* in/out/y row-major with row stride = block.  grid <= 0: default grid.    */
+/* The Gram matvec is two calls: T = w2 ⊙ Xᵀ(a ⊙ V) over the CSC, then     */
+/* W = a ⊙ X T - dinv ⊙ V over the CSR.                                      */
+int sg_spmm(int dtype, int block, int64_t rows, const int64_t* ptr, const int32_t* idx, const float* val,
+            const void* in, void* out, const void* scale, const void* dshift, const void* y, int grid,
+            void* stream);
+
+/* ---- block Krylov-Schur (thick-restart block Lanczos) building blocks --- */
+/* Q: n x ldq row-major basis; W: n x block working block.                   */
+
+/* Number of per-CTA partials of the projections (part = parts*ncols*block). */
+int sg_proj_parts(void);
+
+/* count values uniform in [-0.5, 0.5) from a hash of (seed, index): the    */
+/* start block of the eigensolver, identical on every platform.             */
+int sg_fill_random(int dtype, int64_t count, uint64_t seed, void* out, void* stream);
+
+/* C (ncols x block, FP64) = Q[:, :ncols]ᵀ W.                               */
+int sg_block_proj(int dtype, int block, int64_t n, const void* Q, int64_t ldq, int ncols, const void* W,
+                  double* part, int nparts, double* C, void* stream);
+
+/* W -= Q[:, :ncols] C.                                                      */
+int sg_block_update(int dtype, int block, int64_t n, const void* Q, int64_t ldq, int ncols, const double* C,
+                    void* W, void* stream);
+
+/* One Cholesky-QR pass: G = WᵀW = RᵀR, W <- W R⁻¹ (G, R, Rinv FP64).        */
+/* A rank-deficient block sets status SG_ERR_NUMERIC.                        */
+int sg_block_cholqr(int dtype, int block, int64_t n, void* W, double* part, int nparts, double* G, double* R,
+                    double* Rinv, int* status, void* stream);
+
+/* Q[:, col:col+block] = W; Z = W; Zs = rowscale ⊙ W (NULL pointers skip).   */
+int sg_block_finish(int dtype, int block, int64_t n, const void* W, void* Q, int64_t ldq, int col, void* Z,
+                    void* Zs, const void* rowscale, void* stream);
+
+/* H[m0:m0+b, m0:m0+b] = sym(C1 + C2)[m0:m0+b]; Rout = R2 R1; if            */
+/* write_coupling, H[m0+b:m0+2b, m0:m0+b] = Rout and its transpose.          */
+int sg_lanczos_hblock(int block, double* H, int64_t ldh, int m0, const double* C1, const double* C2,
+                      const double* R1, const double* R2, double* Rout, int write_coupling, void* stream);
+
+/* out[:, 0:k] = Q[:, 0:m] Y[0:m, 0:k] (tq/to: 0 = float, 1 = double).       */
+int sg_basis_rotate(int tq, int to, int64_t n, const void* Q, int64_t ldq, int m, const double* Y,
+                    int64_t ldy, int k, void* out, int64_t ldo, void* stream);
+
+/* ------------------------------------------------------------------------ */
+/* Exact kNN graph -- replaces nearest_neighbour_graph                       */
+/*   (snapatac2-python/src/knn.rs:7-16 -> snapatac2-core/src/utils/knn.rs:  */
+/*   9-31, to_csr_matrix 58-78).                                             */
+/* X: n x d row-major FP64 (d <= 64).  Output: nbr (n x k int64) and dist    */
+/* (n x k FP64 = sqrt of the squared Euclidean distance), each row sorted by */
+/* neighbour index, self excluded by index; identical to the FP64 kNN except */
+/* for the order of exact distance ties (smaller index first).               */
+/* margin: extra FP32 candidates per query (k + margin <= 128 is used).       */
+/* *n_fallback (device int, may be NULL) = number of queries that needed the */
+/* exact FP64 rescan.  scratch: sg_knn_scratch_bytes bytes, 256-B aligned.   */
+/* ------------------------------------------------------------------------ */
+int64_t sg_knn_scratch_bytes(int64_t n, int d, int k, int margin);
+
+int sg_knn(const double* X, int64_t n, int d, int k, int margin, int64_t* nbr, double* dist, void* scratch,
+           int64_t scratch_bytes, int* n_fallback, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

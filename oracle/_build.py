@@ -26,7 +26,7 @@ def build_oracle(force: bool = False) -> None:
             continue
         tmp = so + f".tmp{os.getpid()}"
         procs.append((subprocess.Popen(
-            ["gcc", "-O2", "-fopenmp", "-shared", "-fPIC", s, "-o", tmp, "-lm"]), tmp, so))
+            ["gcc", "-O2", "-ffp-contract=off", "-fopenmp", "-shared", "-fPIC", s, "-o", tmp, "-lm"]), tmp, so))
     for p, tmp, so in procs:
         if p.wait() != 0:
             raise RuntimeError(f"oracle build failed for {so}")

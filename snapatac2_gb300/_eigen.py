@@ -1,0 +1,324 @@
+"""Matrix-free cosine spectral operator and its block Krylov-Schur eigensolver.
+
+Replaces the reference's ``spectral_embedding`` / ``spectral_mf`` / ``eigen``
+(``snapatac2-python/src/embedding.rs:24-59,133-191``): the reference builds an
+owned FP64 CSR, weights it by IDF, L2-normalises the rows, scales them by
+``sqrt(1/(d-1))`` and calls SciPy ARPACK ``eigsh(which='LM')`` on
+``v -> X̂ (X̂ᵀ v) - D⁻¹ v``.
+
+Here X stays on the GPU as an index-only CSR (plus a CSC built once), the
+scalings are folded into two SpMM kernels, and the eigensolver is a
+thick-restart block Lanczos (Krylov-Schur) with full two-pass
+reorthogonalisation:
+
+* block expansion (GPU): W = A Z; two passes of W -= Q (Qᵀ W); two
+  Cholesky-QR passes; the Rayleigh-quotient block and the coupling R are
+  written into H (FP64) on the device;
+* restart (host, FP64 LAPACK): eigendecomposition of the small H, Ritz
+  residuals ||R y||, convergence test, thick restart Q <- Q Y_keep (GPU).
+
+``precision='mixed'`` keeps X, the basis and the SpMM in FP32 with FP32
+accumulation (cross-CTA sums in FP64); H, R, the Ritz problem and the output
+vectors are FP64.  ``precision='fp64'`` runs everything in FP64.
+"""
+from __future__ import annotations
+
+import math
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._binning import DeviceCSR
+
+_DT = {"mixed": (0, torch.float32), "fp64": (1, torch.float64)}
+
+
+@dataclass
+class GramOperator:
+    """A v = a ⊙ (X (w² ⊙ (Xᵀ (a ⊙ v)))) - dinv ⊙ v on the GPU."""
+
+    n: int
+    m: int
+    csr: DeviceCSR
+    colptr: torch.Tensor
+    rowidx: torch.Tensor
+    cvalues: torch.Tensor | None
+    w: torch.Tensor        # FP64 feature weights
+    w2: torch.Tensor       # FP64
+    a: torch.Tensor        # FP64 row scale
+    dinv: torch.Tensor     # FP64
+    w2_32: torch.Tensor
+    a32: torch.Tensor
+    dinv32: torch.Tensor
+    timings: dict = field(default_factory=dict)
+
+    def scales(self, dtype_code: int):
+        if dtype_code == 0:
+            return self.w2_32, self.a32, self.dinv32
+        return self.w2, self.a, self.dinv
+
+    def apply(self, dtype_code: int, block: int, Z, Zs, T, W, stream: int) -> None:
+        """W = A Z (Zs = a ⊙ Z precomputed); T is m x block scratch."""
+        L = _lib.load()
+        w2, a, dinv = self.scales(dtype_code)
+        cv = self.cvalues.data_ptr() if self.cvalues is not None else None
+        v = self.csr.data.data_ptr() if self.csr.data is not None else None
+        _lib.check(L.sg_spmm(dtype_code, block, self.m, self.colptr.data_ptr(), self.rowidx.data_ptr(), cv,
+                             Zs.data_ptr(), T.data_ptr(), w2.data_ptr(), None, None, -1, stream), "sg_spmm (Xᵀ)")
+        _lib.check(L.sg_spmm(dtype_code, block, self.n, self.csr.indptr.data_ptr(), self.csr.indices.data_ptr(), v,
+                             T.data_ptr(), W.data_ptr(), a.data_ptr(), dinv.data_ptr(), Z.data_ptr(), -1, stream),
+                   "sg_spmm (X)")
+
+
+def select_columns(csr: DeviceCSR, features: np.ndarray | None) -> DeviceCSR:
+    """X[:, features] on the GPU (embedding.rs:36-41)."""
+    if features is None:
+        return csr
+    L = _lib.lib()
+    dev = csr.indptr.device
+    n, mfull = csr.shape
+    feats = np.asarray(features)
+    if feats.dtype == bool:
+        if feats.shape[0] != mfull:
+            raise ValueError("feature mask length differs from the number of columns")
+        feats = np.flatnonzero(feats)
+    feats = np.unique(feats.astype(np.int64))
+    colmap = np.full(mfull, -1, dtype=np.int32)
+    colmap[feats] = np.arange(feats.shape[0], dtype=np.int32)
+    cm = torch.from_numpy(colmap).to(dev)
+    nnz = csr.nnz
+    optr = torch.empty(n + 1, dtype=torch.int64, device=dev)
+    oidx = torch.empty(max(nnz, 1), dtype=torch.int32, device=dev)
+    oval = torch.empty(max(nnz, 1), dtype=torch.float32, device=dev) if csr.data is not None else None
+    scan = torch.empty(int(L.sg_scan_scratch_bytes(n + 1)), dtype=torch.uint8, device=dev)
+    sh = torch.cuda.current_stream(dev).cuda_stream
+    _lib.check(L.sg_csr_select_cols(n, csr.indptr.data_ptr(), csr.indices.data_ptr(),
+                                    csr.data.data_ptr() if csr.data is not None else None, cm.data_ptr(),
+                                    optr.data_ptr(), oidx.data_ptr(),
+                                    oval.data_ptr() if oval is not None else None, scan.data_ptr(), sh),
+               "sg_csr_select_cols")
+    k = int(optr[n].item())
+    return DeviceCSR(optr, oidx[:k], oval[:k] if oval is not None else None, (n, int(feats.shape[0])))
+
+
+def build_operator(csr: DeviceCSR, feature_weights=None) -> GramOperator:
+    """Transpose, IDF weights, row norms and degrees (embedding.rs:42-47,139-152)."""
+    L = _lib.lib()
+    dev = csr.indptr.device
+    n, m = csr.shape
+    if n < 2 or m < 1:
+        raise ValueError("need at least 2 cells and 1 feature")
+    sh = torch.cuda.current_stream(dev).cuda_stream
+    st = _lib.DeviceStatus(dev)
+    nblk = int(L.sg_transpose_blocks())
+    nblk = max(1, min(nblk, n))
+    work = torch.empty(nblk * m, dtype=torch.int32, device=dev)
+    colptr = torch.empty(m + 1, dtype=torch.int64, device=dev)
+    rowidx = torch.empty(max(csr.nnz, 1), dtype=torch.int32, device=dev)
+    cval = torch.empty(max(csr.nnz, 1), dtype=torch.float32, device=dev) if csr.data is not None else None
+    scan = torch.empty(int(L.sg_scan_scratch_bytes(max(n, m) + 1)), dtype=torch.uint8, device=dev)
+    vptr = csr.data.data_ptr() if csr.data is not None else None
+    _lib.check(L.sg_csr_transpose(n, m, csr.indptr.data_ptr(), csr.indices.data_ptr(), vptr, nblk,
+                                  work.data_ptr(), colptr.data_ptr(), rowidx.data_ptr(),
+                                  cval.data_ptr() if cval is not None else None, scan.data_ptr(),
+                                  st.status_ptr, sh), "sg_csr_transpose")
+    del work
+    f64 = dict(dtype=torch.float64, device=dev)
+    f32 = dict(dtype=torch.float32, device=dev)
+    w, w2, rinv, colsum = (torch.empty(m, **f64), torch.empty(m, **f64), torch.empty(n, **f64),
+                           torch.empty(m, **f64))
+    a, dinv = torch.empty(n, **f64), torch.empty(n, **f64)
+    w2_32, a32, dinv32 = torch.empty(m, **f32), torch.empty(n, **f32), torch.empty(n, **f32)
+    mm = torch.empty(2, dtype=torch.int64, device=dev)
+    fw = None
+    if feature_weights is not None:
+        fw = torch.as_tensor(np.asarray(feature_weights, dtype=np.float64)).to(dev)
+        if fw.shape[0] != m:
+            raise ValueError(f"feature_weights has {fw.shape[0]} entries, expected {m}")
+    _lib.check(L.sg_spectral_prepare(n, m, csr.indptr.data_ptr(), csr.indices.data_ptr(), vptr,
+                                     colptr.data_ptr(), rowidx.data_ptr(),
+                                     cval.data_ptr() if cval is not None else None,
+                                     fw.data_ptr() if fw is not None else None, w.data_ptr(), w2.data_ptr(),
+                                     w2_32.data_ptr(), rinv.data_ptr(), colsum.data_ptr(), a.data_ptr(),
+                                     dinv.data_ptr(), a32.data_ptr(), dinv32.data_ptr(), mm.data_ptr(),
+                                     st.status_ptr, st.bad_ptr, sh), "sg_spectral_prepare")
+    try:
+        st.raise_if_error("spectral set-up", "cell")
+    except _lib.SnapGB300Error as e:
+        if e.code == _lib.SG_ERR_ARG:
+            raise ValueError("X must be CSR with sorted, unique, in-range column indices") from e
+        if e.code == _lib.SG_ERR_NUMERIC:
+            raise ValueError(f"cell {e.bad_index} has no selected features or shares none with any other "
+                             "cell; the cosine operator is undefined (the reference produces NaN)") from e
+        raise
+    return GramOperator(n, m, csr, colptr, rowidx[:csr.nnz], cval[:csr.nnz] if cval is not None else None,
+                        w, w2, a, dinv, w2_32, a32, dinv32)
+
+
+@dataclass
+class EigenResult:
+    evals: np.ndarray          # k eigenvalues, descending
+    evecs: torch.Tensor        # n x k FP64 on the device
+    info: dict
+
+
+def _default_basis(k: int, block: int, n: int) -> tuple[int, int]:
+    keep = k + max(block * 2, (k + 1) // 2)
+    M = keep + max(8 * block, 96)
+    M = int(math.ceil(M / block) * block)
+    return M, keep
+
+
+def eigsh_lm(op: GramOperator, k: int, *, precision: str = "mixed", block: int = 8, max_basis: int | None = None,
+             keep: int | None = None, tol_vec: float = 1e-9, tol_val: float = 1e-7, vec_positive_only: bool = True,
+             seed: int = 0, max_restarts: int = 200, stream: torch.cuda.Stream | None = None) -> EigenResult:
+    """k eigenpairs of largest magnitude (ARPACK ``which='LM'``) of ``op``.
+
+    Convergence: every wanted Ritz pair must have ||A y - θ y|| <= tol·max|θ|,
+    with ``tol_vec`` for the pairs whose vectors are returned (the positive
+    ones when ``vec_positive_only``, which ``weighted_by_sd`` keeps) and
+    ``tol_val`` for the rest (whose eigenvalues only decide the LM set).
+    """
+    if precision not in _DT:
+        raise ValueError("precision must be 'mixed' or 'fp64'")
+    if block not in (4, 8, 16, 32):
+        raise ValueError("block must be 4, 8, 16 or 32")
+    L = _lib.lib()
+    code, tdt = _DT[precision]
+    n = op.n
+    dev = op.a.device
+    if k < 1 or k >= n:
+        raise ValueError(f"need 1 <= k < n (k={k}, n={n})")
+    if n <= max(4 * (k + block), 2 * block + 64):
+        return _dense_small(op, k, code, tdt, block)
+    M0, keep0 = _default_basis(k, block, n)
+    M = int(max_basis or M0)
+    keep = int(keep or keep0)
+    M = min(M, (n - block) // block * block)
+    keep = min(keep, M - block)
+    if keep < k or M % block:
+        raise ValueError("basis too small for k")
+    s = stream or torch.cuda.current_stream(dev)
+    sh = s.cuda_stream
+    ld = M + block
+    kw = dict(dtype=tdt, device=dev)
+    Q = torch.empty(n, ld, **kw)
+    Q2 = torch.empty(n, ld, **kw)
+    Z, Zs, W = torch.empty(n, block, **kw), torch.empty(n, block, **kw), torch.empty(n, block, **kw)
+    T = torch.empty(op.m, block, **kw)
+    nparts = int(L.sg_proj_parts())
+    f64 = dict(dtype=torch.float64, device=dev)
+    part = torch.empty(nparts * ld * block, **f64)
+    C1, C2 = torch.empty(ld * block, **f64), torch.empty(ld * block, **f64)
+    G = torch.empty(block * block, **f64)
+    R1, R2, Rinv, Rout = (torch.empty(block * block, **f64) for _ in range(4))
+    H = torch.zeros(ld, ld, **f64)
+    st = _lib.DeviceStatus(dev)
+    w2, a, dinv = op.scales(code)
+    t0 = time.perf_counter()
+
+    def cholqr2():
+        _lib.check(L.sg_block_cholqr(code, block, n, W.data_ptr(), part.data_ptr(), nparts, G.data_ptr(),
+                                     R1.data_ptr(), Rinv.data_ptr(), st.status_ptr, sh), "cholqr")
+        _lib.check(L.sg_block_cholqr(code, block, n, W.data_ptr(), part.data_ptr(), nparts, G.data_ptr(),
+                                     R2.data_ptr(), Rinv.data_ptr(), st.status_ptr, sh), "cholqr")
+
+    # start block: deterministic uniform noise, orthonormalised
+    _lib.check(L.sg_fill_random(code, n * block, int(seed) & 0xFFFFFFFFFFFFFFFF, W.data_ptr(), sh), "fill")
+    cholqr2()
+    _lib.check(L.sg_block_finish(code, block, n, W.data_ptr(), Q.data_ptr(), ld, 0, Z.data_ptr(),
+                                 Zs.data_ptr(), a.data_ptr(), sh), "finish")
+    m = 0
+    n_mv = 0
+    restarts = 0
+    hist = []
+    while True:
+        while m + block <= M:
+            op.apply(code, block, Z, Zs, T, W, sh)
+            n_mv += 1
+            ncols = m + block
+            for C in (C1, C2):
+                _lib.check(L.sg_block_proj(code, block, n, Q.data_ptr(), ld, ncols, W.data_ptr(), part.data_ptr(),
+                                           nparts, C.data_ptr(), sh), "proj")
+                _lib.check(L.sg_block_update(code, block, n, Q.data_ptr(), ld, ncols, C.data_ptr(),
+                                             W.data_ptr(), sh), "update")
+            cholqr2()
+            _lib.check(L.sg_lanczos_hblock(block, H.data_ptr(), ld, m, C1.data_ptr(), C2.data_ptr(), R1.data_ptr(),
+                                           R2.data_ptr(), Rout.data_ptr(), 1, sh), "hblock")
+            _lib.check(L.sg_block_finish(code, block, n, W.data_ptr(), Q.data_ptr(), ld, m + block, Z.data_ptr(),
+                                         Zs.data_ptr(), a.data_ptr(), sh), "finish")
+            m += block
+        # after a thick restart keep need not be a multiple of the block, so
+        # the basis ends at m (<= M): the Ritz problem is H[:m, :m]
+        Me = m
+        Hh = H.cpu().numpy()
+        st.raise_if_error("block Lanczos (rank-deficient Krylov block)")
+        th, Y = np.linalg.eigh(Hh[:Me, :Me])
+        Rl = Hh[Me:Me + block, Me - block:Me]
+        res = np.linalg.norm(Rl @ Y[Me - block:Me, :], axis=0)
+        order = np.argsort(-np.abs(th), kind="stable")
+        sel = order[:k]
+        anorm = max(float(np.abs(th).max()), 1e-300)
+        need = np.where((th[sel] > 0) | (not vec_positive_only), tol_vec, tol_val) * anorm
+        worst = float(np.max(res[sel] / need))
+        hist.append(float(res[sel].max()))
+        if worst <= 1.0 or restarts >= max_restarts:
+            break
+        if precision == "mixed" and len(hist) >= 6 and min(hist[-3:]) > 0.7 * min(hist[:-3]):
+            break  # FP32 floor reached: no further progress
+        restarts += 1
+        kp = order[:keep]
+        Yk = torch.from_numpy(np.ascontiguousarray(Y[:, kp])).to(dev)
+        _lib.check(L.sg_basis_rotate(code, code, n, Q.data_ptr(), ld, Me, Yk.data_ptr(), keep, keep, Q2.data_ptr(),
+                                     ld, sh), "rotate")
+        _lib.check(L.sg_block_finish(code, block, n, Z.data_ptr(), Q2.data_ptr(), ld, keep, None, None, None, sh),
+                   "finish")
+        Q, Q2 = Q2, Q
+        Hn = np.zeros((ld, ld))
+        Hn[np.arange(keep), np.arange(keep)] = th[kp]
+        Bc = Rl @ Y[Me - block:Me, kp]
+        Hn[keep:keep + block, :keep] = Bc
+        Hn[:keep, keep:keep + block] = Bc.T
+        H.copy_(torch.from_numpy(Hn))
+        m = keep
+    # Ritz vectors (FP64 output), eigenvalues sorted descending like the reference
+    sel = order[:k]
+    sel = sel[np.argsort(-th[sel], kind="stable")]
+    Yk = torch.from_numpy(np.ascontiguousarray(Y[:, sel])).to(dev)
+    U = torch.empty(n, k, **f64)
+    _lib.check(L.sg_basis_rotate(code, 1, n, Q.data_ptr(), ld, Me, Yk.data_ptr(), k, k, U.data_ptr(), k, sh),
+               "rotate")
+    torch.cuda.synchronize(dev)
+    info = dict(block_matvecs=n_mv, vector_matvecs=n_mv * block, restarts=restarts, basis=M, keep=keep,
+                residuals=res[sel].tolist(), converged=worst <= 1.0, seconds=time.perf_counter() - t0,
+                precision=precision, block=block)
+    return EigenResult(th[sel].copy(), U, info)
+
+
+def _dense_small(op: GramOperator, k: int, code: int, tdt, block: int) -> EigenResult:
+    """Tiny problems: apply A to the identity on the GPU and solve densely."""
+    L = _lib.load()
+    n, dev = op.n, op.a.device
+    sh = torch.cuda.current_stream(dev).cuda_stream
+    kw = dict(dtype=tdt, device=dev)
+    w2, a, dinv = op.scales(code)
+    A = np.zeros((n, n))
+    Z, Zs, W = (torch.zeros(n, block, **kw) for _ in range(3))
+    T = torch.empty(op.m, block, **kw)
+    for c0 in range(0, n, block):
+        Z.zero_()
+        cols = min(block, n - c0)
+        Z[torch.arange(c0, c0 + cols, device=dev), torch.arange(cols, device=dev)] = 1
+        _lib.check(L.sg_block_finish(code, block, n, Z.data_ptr(), None, 0, 0, None, Zs.data_ptr(), a.data_ptr(),
+                                     sh), "finish")
+        op.apply(code, block, Z, Zs, T, W, sh)
+        A[:, c0:c0 + cols] = W[:, :cols].double().cpu().numpy()
+    A = 0.5 * (A + A.T)
+    th, Y = np.linalg.eigh(A)
+    order = np.argsort(-np.abs(th), kind="stable")[:k]
+    order = order[np.argsort(-th[order], kind="stable")]
+    U = torch.from_numpy(np.ascontiguousarray(Y[:, order])).to(dev)
+    return EigenResult(th[order].copy(), U, dict(dense=True, n=n, block_matvecs=(n + block - 1) // block))

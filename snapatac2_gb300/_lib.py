@@ -40,6 +40,22 @@ SIGNATURES: dict[str, tuple] = {
     "sg_tile_run": (_I32, [_P, _I64, _I64, _P, _P, _P, _P, _P, _I32, _U32, _I32, _I64, _I64, _P, _P,
                            _I64, _P, _P, _P, _P, _P]),
     "sg_tile_emit": (_I32, [_I64, _P, _P, _I64, _P, _P, _P, _I64, _P, _P]),
+    "sg_csr_select_cols": (_I32, [_I64, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
+    "sg_transpose_blocks": (_I32, []),
+    "sg_csr_transpose": (_I32, [_I64, _I64, _P, _P, _P, _I32, _P, _P, _P, _P, _P, _P, _P]),
+    "sg_spectral_prepare": (_I32, [_I64, _I64, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P,
+                                   _P, _P, _P, _P, _P, _P]),
+    "sg_spmm": (_I32, [_I32, _I32, _I64, _P, _P, _P, _P, _P, _P, _P, _P, _I32, _P]),
+    "sg_proj_parts": (_I32, []),
+    "sg_fill_random": (_I32, [_I32, _I64, ctypes.c_uint64, _P, _P]),
+    "sg_block_proj": (_I32, [_I32, _I32, _I64, _P, _I64, _I32, _P, _P, _I32, _P, _P]),
+    "sg_block_update": (_I32, [_I32, _I32, _I64, _P, _I64, _I32, _P, _P, _P]),
+    "sg_block_cholqr": (_I32, [_I32, _I32, _I64, _P, _P, _I32, _P, _P, _P, _P, _P]),
+    "sg_block_finish": (_I32, [_I32, _I32, _I64, _P, _P, _I64, _I32, _P, _P, _P, _P]),
+    "sg_lanczos_hblock": (_I32, [_I32, _P, _I64, _I32, _P, _P, _P, _P, _P, _I32, _P]),
+    "sg_knn_scratch_bytes": (_I64, [_I64, _I32, _I32, _I32]),
+    "sg_knn": (_I32, [_P, _I64, _I32, _I32, _I32, _P, _P, _P, _I64, _P, _P]),
+    "sg_basis_rotate": (_I32, [_I32, _I32, _I64, _P, _I64, _I32, _P, _I64, _I32, _P, _I64, _P]),
 }
 
 _lock = threading.Lock()

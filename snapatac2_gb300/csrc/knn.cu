@@ -1,0 +1,430 @@
+// Exact Euclidean k-nearest-neighbour graph, replacing the reference's
+// kd-tree search (snapatac2-core/src/utils/knn.rs:9-31: squared Euclidean in
+// FP64, self removed by index, first k kept, value = sqrt(distance); rows of
+// the CSR sorted by column index, to_csr_matrix 58-78).
+//
+// Pipeline (no host synchronisation):
+//  1. prep    X (n x d FP64) -> zero-padded FP32 and FP64 copies (n x DP),
+//             max row norm.
+//  2. scan    tiled brute force in FP32: a CTA owns 32 queries (one per lane,
+//             query vector in registers) and streams 128-candidate tiles
+//             through shared memory; each warp computes 32 x 16 distances
+//             with broadcast float4 loads, then a fused warp-level top-K'
+//             selection (K' = k + margin) keeps per-query candidate lists in
+//             shared memory: candidates below the current K'-th distance are
+//             appended by ballot and the list is re-sorted (warp bitonic)
+//             when it overflows.
+//  3. rerank  FP64 distances of the K' candidates, sort by (distance, index),
+//             keep k.  Certificate: every point outside the list has FP32
+//             distance >= tau (the K'-th), hence FP64 distance >= tau - delta
+//             with delta a bound on the FP32 error; if tau - delta > the k-th
+//             FP64 distance the FP64 top-k is exact, otherwise the query is
+//             queued for
+//  4. exact   the same scan in FP64 for the queued queries only.
+//  5. rows sorted by column index, distances sqrt'ed.
+// Ties are broken by the smaller index.
+#include <float.h>
+
+#include <type_traits>
+
+#include "common.cuh"
+#include "internal.h"
+
+namespace sg {
+namespace {
+
+constexpr int kQT = 32;    // queries per CTA (one per lane)
+constexpr int kCT = 128;   // candidates per shared-memory tile
+constexpr int kLW = 8;     // warps per CTA
+constexpr int kList = 256; // per-query list + append buffer
+constexpr int kMaxKp = 128;
+
+template <typename K>
+__device__ __forceinline__ bool lex_gt(K a, int ia, K b, int ib) {
+  return a > b || (a == b && ia > ib);
+}
+
+// Ascending bitonic sort of N = 2^p (key, idx) pairs in shared memory by one warp.
+template <typename K>
+__device__ void warp_bitonic(K* key, int* idx, int N) {
+  const int lane = threadIdx.x & 31;
+  for (int size = 2; size <= N; size <<= 1) {
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      for (int t = lane; t < (N >> 1); t += 32) {
+        const int i = 2 * t - (t & (stride - 1));
+        const int j = i + stride;
+        const bool asc = (i & size) == 0;
+        const K ki = key[i], kj = key[j];
+        const int ii = idx[i], ij = idx[j];
+        if (lex_gt(ki, ii, kj, ij) == asc) {
+          key[i] = kj; key[j] = ki;
+          idx[i] = ij; idx[j] = ii;
+        }
+      }
+      __syncwarp();
+    }
+  }
+}
+
+template <typename K> __device__ __forceinline__ K kinf();
+template <> __device__ __forceinline__ float kinf<float>() { return FLT_MAX; }
+template <> __device__ __forceinline__ double kinf<double>() { return DBL_MAX; }
+
+template <typename TD, int DP>
+struct ScanSmem {
+  TD cv[kCT][DP];          // candidate tile
+  TD dist[kQT][kCT + 1];   // distance tile
+  TD lk[kQT][kList];       // per-query list keys
+  int li[kQT][kList];      // per-query list indices
+  int cnt[kQT];
+  TD tau[kQT];
+};
+
+// Sort query q's list (warp), keep Kp, update tau.
+template <typename TD, int DP>
+__device__ void merge_list(ScanSmem<TD, DP>& sm, int q, int Kp) {
+  const int lane = threadIdx.x & 31;
+  const int c = sm.cnt[q];
+  for (int t = c + lane; t < kList; t += 32) {
+    sm.lk[q][t] = kinf<TD>();
+    sm.li[q][t] = 0x7fffffff;
+  }
+  __syncwarp();
+  warp_bitonic<TD>(sm.lk[q], sm.li[q], kList);
+  __syncwarp();
+  if (lane == 0) {
+    const int keep = c < Kp ? c : Kp;
+    sm.cnt[q] = keep;
+    sm.tau[q] = keep == Kp ? sm.lk[q][Kp - 1] : kinf<TD>();
+  }
+  __syncwarp();
+}
+
+// Scan all n points for queries qlist[blockIdx.x*32 + lane] (or the identity
+// when qlist == nullptr).  Writes per query the Kp best (distance, index)
+// sorted ascending, and tau = Kp-th distance (inf if fewer).
+template <typename TD, int DP>
+__global__ void __launch_bounds__(kLW * 32)
+scan_kernel(const TD* __restrict__ Xp, int64_t n, const int* __restrict__ qlist, const int* __restrict__ qcount,
+            int Kp, int* __restrict__ cand, TD* __restrict__ cand_d, TD* __restrict__ tau_out) {
+  extern __shared__ __align__(16) unsigned char sraw[];
+  ScanSmem<TD, DP>& sm = *reinterpret_cast<ScanSmem<TD, DP>*>(sraw);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int64_t nq = qcount ? (int64_t)*qcount : n;
+  const int64_t qbase = (int64_t)blockIdx.x * kQT;
+  if (qbase >= nq) return;  // uniform across the CTA
+  const int64_t qslot = qbase + lane;
+  const bool qvalid = qslot < nq;
+  const int64_t qid = qvalid ? (qlist ? (int64_t)qlist[qslot] : qslot) : -1;
+
+  using V = typename std::conditional<sizeof(TD) == 4, float4, double2>::type;
+  constexpr int VW = 16 / sizeof(TD);
+  TD qr[DP];
+#pragma unroll
+  for (int t = 0; t < DP; t += VW) {
+    V v;
+    if (qvalid) v = *reinterpret_cast<const V*>(Xp + qid * DP + t);
+    else memset(&v, 0, sizeof(v));
+    const TD* pv = reinterpret_cast<const TD*>(&v);
+#pragma unroll
+    for (int s = 0; s < VW; ++s) qr[t + s] = pv[s];
+  }
+  if (threadIdx.x < kQT) {
+    sm.cnt[threadIdx.x] = 0;
+    sm.tau[threadIdx.x] = kinf<TD>();
+  }
+  for (int64_t c0 = 0; c0 < n; c0 += kCT) {
+    __syncthreads();
+    // load candidate tile
+    const int nct = (n - c0) < kCT ? (int)(n - c0) : kCT;
+    for (int t = threadIdx.x; t < kCT * DP / VW; t += kLW * 32) {
+      const int r = t / (DP / VW), v = t % (DP / VW);
+      V val;
+      if (r < nct) val = *reinterpret_cast<const V*>(Xp + (c0 + r) * DP + v * VW);
+      else memset(&val, 0, sizeof(val));
+      *reinterpret_cast<V*>(&sm.cv[r][v * VW]) = val;
+    }
+    __syncthreads();
+    // distances: lane = query, warp covers candidates wid, wid+8, ...
+#pragma unroll 2
+    for (int j = 0; j < kCT / kLW; ++j) {
+      const int c = wid + j * kLW;
+      TD acc = TD(0);
+#pragma unroll
+      for (int t = 0; t < DP; t += VW) {
+        const V v = *reinterpret_cast<const V*>(&sm.cv[c][t]);
+        const TD* pv = reinterpret_cast<const TD*>(&v);
+#pragma unroll
+        for (int s = 0; s < VW; ++s) {
+          if (sizeof(TD) == 8) {  // FP64 pass: the reference's unfused arithmetic
+            const double df = __dsub_rn((double)qr[t + s], (double)pv[s]);
+            acc = (TD)__dadd_rn((double)acc, __dmul_rn(df, df));
+          } else {
+            const TD df = qr[t + s] - pv[s];
+            acc = fma(df, df, acc);
+          }
+        }
+      }
+      const int64_t cg = c0 + c;
+      if (c >= nct || cg == qid || !qvalid) acc = kinf<TD>();
+      sm.dist[lane][c] = acc;
+    }
+    __syncthreads();
+    // fused selection: warp wid owns queries 4*wid .. 4*wid+3
+    for (int qq = 0; qq < kQT / kLW; ++qq) {
+      const int q = wid * (kQT / kLW) + qq;
+      const TD th = sm.tau[q];
+      int base = sm.cnt[q];
+#pragma unroll
+      for (int j = 0; j < kCT / 32; ++j) {
+        const int c = lane + 32 * j;
+        const TD dv = sm.dist[q][c];
+        const bool take = dv < th;
+        const unsigned bal = __ballot_sync(0xffffffffu, take);
+        if (take) {
+          const int p = base + __popc(bal & lanemask_lt());
+          sm.lk[q][p] = dv;
+          sm.li[q][p] = (int)(c0 + c);
+        }
+        base += __popc(bal);
+      }
+      __syncwarp();
+      if (lane == 0) sm.cnt[q] = base;
+      __syncwarp();
+      if (base > kList - kCT) merge_list<TD, DP>(sm, q, Kp);
+    }
+  }
+  __syncthreads();
+  for (int qq = 0; qq < kQT / kLW; ++qq) {
+    const int q = wid * (kQT / kLW) + qq;
+    merge_list<TD, DP>(sm, q, Kp);
+    const int64_t qs = qbase + q;
+    if (qs < nq) {
+      const int c = sm.cnt[q];
+      for (int t = lane; t < Kp; t += 32) {
+        cand[qs * Kp + t] = t < c ? sm.li[q][t] : -1;
+        if (cand_d) cand_d[qs * Kp + t] = t < c ? sm.lk[q][t] : kinf<TD>();
+      }
+      if (lane == 0 && tau_out) tau_out[qs] = sm.tau[q];
+    }
+  }
+}
+
+// X (n x d FP64) -> padded FP32 / FP64 copies; max row norm (as float bits)
+template <int DP>
+__global__ void prep_kernel(const double* __restrict__ X, int64_t n, int d, float* __restrict__ X32,
+                            double* __restrict__ X64, unsigned* __restrict__ maxnorm_bits) {
+  float mx = 0.f;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    double s = 0.0;
+#pragma unroll 4
+    for (int t = 0; t < DP; ++t) {
+      const double v = t < d ? X[i * d + t] : 0.0;
+      X32[i * DP + t] = (float)v;
+      X64[i * DP + t] = v;
+      s += v * v;
+    }
+    mx = fmaxf(mx, (float)sqrt(s) * 1.0000002f);
+  }
+  for (int o = 16; o; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(maxnorm_bits, __float_as_uint(mx));
+}
+
+// Write row q: the k (distance, index) pairs in kd[0..k) / ki[0..k) (any
+// order) sorted by column index, distances sqrt'ed.  Uses kk/ks scratch.
+__device__ void emit_row(int64_t q, int k, const double* kd, const int* kidx, double* kk, int* ks,
+                         int64_t* __restrict__ nbr, double* __restrict__ dist) {
+  const int lane = threadIdx.x & 31;
+  for (int s = lane; s < kMaxKp; s += 32) {
+    kk[s] = s < k ? (double)kidx[s] : DBL_MAX;
+    ks[s] = s < k ? s : 0x7fffffff;
+  }
+  __syncwarp();
+  warp_bitonic<double>(kk, ks, kMaxKp);
+  for (int t = lane; t < k; t += 32) {
+    nbr[q * k + t] = (int64_t)kk[t];
+    dist[q * k + t] = sqrt(kd[ks[t]]);
+  }
+  __syncwarp();
+}
+
+// FP64 re-rank of the Kp FP32 candidates (warp per query), certificate check.
+template <int DP>
+__global__ void __launch_bounds__(256)
+rerank_kernel(const double* __restrict__ X64, int64_t n, int d, const int* __restrict__ cand, int Kp,
+              const float* __restrict__ tau32, int k, const unsigned* __restrict__ maxnorm_bits,
+              int64_t* __restrict__ nbr, double* __restrict__ dist, int* __restrict__ flagged,
+              int* __restrict__ nflag) {
+  __shared__ double kd[8][kMaxKp];
+  __shared__ int kc[8][kMaxKp];
+  __shared__ double tk[8][kMaxKp];
+  __shared__ int ts[8][kMaxKp];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int64_t q = (int64_t)blockIdx.x * 8 + w;
+  if (q >= n) return;
+  const double* xq = X64 + q * DP;
+  double qn = 0.0;
+  for (int t = 0; t < d; ++t) qn = fma(xq[t], xq[t], qn);
+  qn = sqrt(qn);
+  for (int s = lane; s < kMaxKp; s += 32) {
+    const int c = s < Kp ? cand[q * Kp + s] : -1;
+    double dd = DBL_MAX;
+    if (c >= 0) {
+      const double* xc = X64 + (int64_t)c * DP;
+      // sequential, unfused sum of squares: the reference's squared_euclidean
+      dd = 0.0;
+      for (int t = 0; t < d; ++t) {
+        const double df = __dsub_rn(xq[t], xc[t]);
+        dd = __dadd_rn(dd, __dmul_rn(df, df));
+      }
+    }
+    kd[w][s] = dd;
+    kc[w][s] = c >= 0 ? c : 0x7fffffff;
+  }
+  __syncwarp();
+  warp_bitonic<double>(kd[w], kc[w], kMaxKp);
+  // Certificate: every point j outside the list has d32(j) >= tau32, and
+  // |d32 - d64| <= delta = (d + 8) * 2^-22 * (|x_q| + max|x|)^2 (rounding of
+  // the inputs to FP32 and of the FP32 sum of squares).
+  const double mx = (double)__uint_as_float(*maxnorm_bits);
+  const double delta = (double)(d + 8) * 2.384185791015625e-07 * (qn + mx) * (qn + mx);
+  const double t32 = (double)tau32[q];
+  const double dk = kd[w][k - 1];
+  const bool full = kc[w][k - 1] != 0x7fffffff;
+  const bool all_seen = t32 >= 3.0e38;  // fewer than Kp points: every point is a candidate
+  const bool exact = full && (all_seen || t32 - delta > dk);
+  if (!exact) {
+    if (lane == 0) flagged[atomicAdd(nflag, 1)] = (int)q;
+    return;
+  }
+  emit_row(q, k, kd[w], kc[w], tk[w], ts[w], nbr, dist);
+}
+
+// Rows of the queries that the certificate rejected, from the exact FP64 scan.
+__global__ void __launch_bounds__(256)
+finalize_kernel(const int* __restrict__ flagged, const int* __restrict__ nflag, const int* __restrict__ cand,
+                const double* __restrict__ cand_d, int k, int64_t* __restrict__ nbr, double* __restrict__ dist) {
+  __shared__ double kd[8][kMaxKp];
+  __shared__ int kc[8][kMaxKp];
+  __shared__ double tk[8][kMaxKp];
+  __shared__ int ts[8][kMaxKp];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int64_t slot = (int64_t)blockIdx.x * 8 + w;
+  if (slot >= *nflag) return;
+  const int64_t q = flagged[slot];
+  for (int s = lane; s < k; s += 32) {
+    kd[w][s] = cand_d[slot * k + s];
+    kc[w][s] = cand[slot * k + s];
+  }
+  __syncwarp();
+  emit_row(q, k, kd[w], kc[w], tk[w], ts[w], nbr, dist);
+}
+
+__global__ void zero_int(int* p, unsigned* u) {
+  *p = 0;
+  *u = 0u;
+}
+
+struct KnnScratch {
+  float* X32;
+  double* X64;
+  int* cand;
+  float* tau32;
+  int* flagged;
+  int* fcand;
+  double* fcand_d;
+  int* nflag;
+  unsigned* maxnorm;
+  int64_t bytes;
+};
+
+inline int64_t align256(int64_t x) { return (x + 255) / 256 * 256; }
+
+KnnScratch knn_layout(char* base, int64_t n, int DP, int k, int Kp) {
+  KnnScratch s{};
+  int64_t o = 0;
+  auto take = [&](int64_t b) { int64_t r = o; o += align256(b); return r; };
+  const int64_t oX32 = take(n * DP * 4), oX64 = take(n * DP * 8), oc = take(n * (int64_t)Kp * 4),
+                ot = take(n * 4), of = take(n * 4), ofc = take(n * (int64_t)k * 4),
+                ofd = take(n * (int64_t)k * 8), on = take(16);
+  if (base) {
+    s.X32 = (float*)(base + oX32);
+    s.X64 = (double*)(base + oX64);
+    s.cand = (int*)(base + oc);
+    s.tau32 = (float*)(base + ot);
+    s.flagged = (int*)(base + of);
+    s.fcand = (int*)(base + ofc);
+    s.fcand_d = (double*)(base + ofd);
+    s.nflag = (int*)(base + on);
+    s.maxnorm = (unsigned*)(base + on + 8);
+  }
+  s.bytes = o;
+  return s;
+}
+
+inline int pad_dim(int d) { return d <= 16 ? 16 : (d <= 32 ? 32 : 64); }
+
+template <typename TD, int DP>
+int launch_scan(const TD* Xp, int64_t n, const int* qlist, const int* qcount, int Kp, int* cand, TD* cand_d,
+                TD* tau, cudaStream_t s) {
+  const size_t smem = sizeof(ScanSmem<TD, DP>);
+  if (cudaFuncSetAttribute(scan_kernel<TD, DP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+      cudaSuccess)
+    return SG_ERR_CUDA;
+  const int64_t grid = (n + kQT - 1) / kQT;
+  scan_kernel<TD, DP><<<(unsigned)grid, kLW * 32, smem, s>>>(Xp, n, qlist, qcount, Kp, cand, cand_d, tau);
+  return cudaGetLastError() == cudaSuccess ? SG_OK : SG_ERR_CUDA;
+}
+
+template <int DP>
+int knn_run(const double* X, int64_t n, int d, int k, int Kp, const KnnScratch& w, int64_t* nbr, double* dist,
+            cudaStream_t s) {
+  zero_int<<<1, 1, 0, s>>>(w.nflag, w.maxnorm);
+  prep_kernel<DP><<<grid_for(n, 256, 4096), 256, 0, s>>>(X, n, d, w.X32, w.X64, w.maxnorm);
+  SG_CHECK_LAUNCH();
+  int e = launch_scan<float, DP>(w.X32, n, nullptr, nullptr, Kp, w.cand, nullptr, w.tau32, s);
+  if (e) return e;
+  rerank_kernel<DP><<<(unsigned)((n + 7) / 8), 256, 0, s>>>(w.X64, n, d, w.cand, Kp, w.tau32, k, w.maxnorm, nbr,
+                                                            dist, w.flagged, w.nflag);
+  SG_CHECK_LAUNCH();
+  // exact FP64 scan of the rejected queries (CTAs past the count exit at once)
+  e = launch_scan<double, DP>(w.X64, n, w.flagged, w.nflag, k, w.fcand, w.fcand_d, nullptr, s);
+  if (e) return e;
+  finalize_kernel<<<(unsigned)((n + 7) / 8), 256, 0, s>>>(w.flagged, w.nflag, w.fcand, w.fcand_d, k, nbr, dist);
+  SG_CHECK_LAUNCH();
+  return SG_OK;
+}
+
+}  // namespace
+}  // namespace sg
+
+using namespace sg;
+
+extern "C" int64_t sg_knn_scratch_bytes(int64_t n, int d, int k, int margin) {
+  if (n <= 0 || d <= 0 || d > 64 || k <= 0 || margin < 0) return -1;
+  const int Kp = k + margin;
+  return knn_layout(nullptr, n, pad_dim(d), k, Kp).bytes;
+}
+
+extern "C" int sg_knn(const double* X, int64_t n, int d, int k, int margin, int64_t* nbr, double* dist,
+                      void* scratch, int64_t scratch_bytes, int* n_fallback, void* stream) {
+  if (n < 2 || d <= 0 || d > 64 || k <= 0 || k > n - 1 || margin < 0 || n > 0x7fffffffLL) return SG_ERR_ARG;
+  int Kp = k + margin;
+  if (Kp > kMaxKp) Kp = kMaxKp;
+  if (Kp > n - 1) Kp = (int)(n - 1);
+  if (k > Kp) return SG_ERR_ARG;
+  if (((uintptr_t)scratch & 255u) != 0) return SG_ERR_ARG;
+  const int DP = pad_dim(d);
+  KnnScratch w = knn_layout((char*)scratch, n, DP, k, k + margin);
+  if (scratch_bytes < w.bytes) return SG_ERR_CAP;
+  cudaStream_t s = as_stream(stream);
+  int e;
+  if (DP == 16) e = knn_run<16>(X, n, d, k, Kp, w, nbr, dist, s);
+  else if (DP == 32) e = knn_run<32>(X, n, d, k, Kp, w, nbr, dist, s);
+  else e = knn_run<64>(X, n, d, k, Kp, w, nbr, dist, s);
+  if (e) return e;
+  if (n_fallback &&
+      cudaMemcpyAsync(n_fallback, w.nflag, sizeof(int), cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+    return SG_ERR_CUDA;
+  return SG_OK;
+}

@@ -1,0 +1,435 @@
+// Dense block kernels of the thick-restart block Lanczos (Krylov-Schur)
+// eigensolver that replaces the reference's ARPACK call
+// (snapatac2-python/src/embedding.rs:155-171, eigsh which='LM').
+//
+// Layout: the basis Q is n x ldq row-major (each cell's basis coefficients
+// contiguous), the working block W is n x B row-major.  T = float (mixed
+// precision) or double (all-FP64).  Every reduction across rows goes through
+// per-CTA partials summed in a fixed order in FP64, so results are
+// bit-reproducible run to run.
+//
+//   proj    C = Q[:, :ncols]ᵀ W           (ncols x B, FP64)
+//   update  W -= Q[:, :ncols] C
+//   cholqr  G = WᵀW, G = RᵀR (FP64 Cholesky), W <- W R⁻¹
+//   finish  Q[:, col:col+B] = W, Z = W, Zs = a ⊙ W
+//   hblock  Rayleigh-quotient diagonal block and coupling R into H (FP64)
+//   rotate  out = Q[:, :m] Y                (thick restart, Ritz vectors)
+#include "common.cuh"
+#include "internal.h"
+
+namespace sg {
+namespace {
+
+constexpr int kProjBlock = 256;
+constexpr int kProjRows = 32;
+
+int sm_count_l() {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  return sms > 0 ? sms : 1;
+}
+
+// part[blk][p][c] = sum over this CTA's rows of Q[i,p] W[i,c]
+template <typename T, int B, int CPT>
+__global__ void __launch_bounds__(kProjBlock)
+proj_partial(int64_t n, const T* __restrict__ Q, int64_t ldq, int ncols, const T* __restrict__ W,
+             double* __restrict__ part) {
+  __shared__ T ws[kProjRows][B];
+  const int nb = gridDim.x, b = blockIdx.x;
+  const int64_t r0 = n * b / nb, r1 = n * (b + 1) / nb;
+  T acc[CPT][B];
+#pragma unroll
+  for (int q = 0; q < CPT; ++q)
+#pragma unroll
+    for (int c = 0; c < B; ++c) acc[q][c] = T(0);
+  for (int64_t base = r0; base < r1; base += kProjRows) {
+    const int nr = (r1 - base) < kProjRows ? (int)(r1 - base) : kProjRows;
+    __syncthreads();
+    for (int t = threadIdx.x; t < kProjRows * B; t += kProjBlock) {
+      const int i = t / B, c = t % B;
+      ws[i][c] = i < nr ? W[(base + i) * B + c] : T(0);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < CPT; ++q) {
+      const int p = threadIdx.x + q * kProjBlock;
+      if (p < ncols) {
+        for (int i = 0; i < nr; ++i) {
+          const T qv = Q[(base + i) * ldq + p];
+#pragma unroll
+          for (int c = 0; c < B; ++c) acc[q][c] = fma(qv, ws[i][c], acc[q][c]);
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < CPT; ++q) {
+    const int p = threadIdx.x + q * kProjBlock;
+    if (p < ncols) {
+#pragma unroll
+      for (int c = 0; c < B; ++c) part[((int64_t)b * ncols + p) * B + c] = (double)acc[q][c];
+    }
+  }
+}
+
+__global__ void proj_reduce(int nparts, int ncols, int B, const double* __restrict__ part, double* __restrict__ C) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int tot = ncols * B;
+  if (t >= tot) return;
+  double s = 0.0;
+  for (int b = 0; b < nparts; ++b) s += part[(int64_t)b * tot + t];
+  C[t] = s;
+}
+
+// W[i,:] -= Q[i, :ncols] C   (one warp per row; lanes over basis columns)
+template <typename T, int B>
+__global__ void __launch_bounds__(256)
+update_kernel(int64_t n, const T* __restrict__ Q, int64_t ldq, int ncols, const double* __restrict__ C,
+              T* __restrict__ W) {
+  extern __shared__ __align__(16) unsigned char sraw[];
+  T* cs = reinterpret_cast<T*>(sraw);  // ncols x B
+  for (int t = threadIdx.x; t < ncols * B; t += blockDim.x) cs[t] = (T)C[t];
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t i = gw; i < n; i += nw) {
+    T acc[B];
+#pragma unroll
+    for (int c = 0; c < B; ++c) acc[c] = T(0);
+    for (int p = lane; p < ncols; p += 32) {
+      const T qv = Q[i * ldq + p];
+#pragma unroll
+      for (int c = 0; c < B; ++c) acc[c] = fma(qv, cs[p * B + c], acc[c]);
+    }
+#pragma unroll
+    for (int c = 0; c < B; ++c) {
+      T v = acc[c];
+#pragma unroll
+      for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      acc[c] = v;
+    }
+    // lane c writes column c (B <= 32)
+    T mine = T(0);
+#pragma unroll
+    for (int c = 0; c < B; ++c) if (lane == c) mine = acc[c];
+    if (lane < B) W[i * B + lane] -= mine;
+  }
+}
+
+// Cholesky of the B x B Gram matrix (one warp, lane j owns column j):
+// G = RᵀR with R upper triangular; also Rinv = R⁻¹.  A non-positive pivot
+// relative to the diagonal sets SG_ERR_NUMERIC (rank-deficient block).
+__global__ void chol_kernel(int B, const double* __restrict__ G, double* __restrict__ R,
+                            double* __restrict__ Rinv, int* status) {
+  __shared__ double r[32][33];
+  const int j = threadIdx.x;
+  for (int i = 0; i < B; ++i) r[i][j] = 0.0;
+  __syncwarp();
+  bool fail = false;
+  for (int k = 0; k < B; ++k) {
+    double piv = 0.0;
+    if (j == k) {
+      double s = G[k * B + k];
+      for (int i = 0; i < k; ++i) s -= r[i][k] * r[i][k];
+      const double gkk = G[k * B + k];
+      if (!(s > 1e-28 * (gkk > 0 ? gkk : 1.0)) || !(s > 0.0)) { fail = true; s = 1.0; }
+      r[k][k] = sqrt(s);
+    }
+    __syncwarp();
+    piv = r[k][k];
+    if (j > k && j < B) {
+      double s = G[k * B + j];
+      for (int i = 0; i < k; ++i) s -= r[i][k] * r[i][j];
+      r[k][j] = s / piv;
+    }
+    __syncwarp();
+  }
+  if (__any_sync(0xffffffffu, fail) && j == 0) atomicCAS(status, 0, SG_ERR_NUMERIC);
+  // back substitution, lane j computes column j of R^-1
+  if (j < B) {
+    double x[32];
+    for (int i = 0; i < 32; ++i) x[i] = 0.0;
+    x[j] = 1.0 / r[j][j];
+    for (int i = j - 1; i >= 0; --i) {
+      double s = 0.0;
+      for (int t = i + 1; t <= j; ++t) s += r[i][t] * x[t];
+      x[i] = -s / r[i][i];
+    }
+    for (int i = 0; i < B; ++i) {
+      Rinv[i * B + j] = i <= j ? x[i] : 0.0;
+      R[i * B + j] = r[i][j];
+    }
+  }
+}
+
+// W[i,:] <- W[i,:] Rinv   (warp per row, lane c computes column c)
+template <typename T, int B>
+__global__ void __launch_bounds__(256) apply_rinv(int64_t n, const double* __restrict__ Rinv, T* __restrict__ W) {
+  __shared__ T ri[B][B];
+  for (int t = threadIdx.x; t < B * B; t += blockDim.x) ri[t / B][t % B] = (T)Rinv[t];
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t i = gw; i < n; i += nw) {
+    const T w = lane < B ? W[i * B + lane] : T(0);
+    T s = T(0);
+#pragma unroll
+    for (int k = 0; k < B; ++k) {
+      const T wk = __shfl_sync(0xffffffffu, w, k);
+      if (lane < B && k <= lane) s = fma(wk, ri[k][lane < B ? lane : 0], s);
+    }
+    if (lane < B) W[i * B + lane] = s;
+  }
+}
+
+// Q[i, col:col+B] = W[i,:]; Z = W (optional); Zs = a ⊙ W
+template <typename T>
+__global__ void finish_kernel(int64_t n, int B, const T* __restrict__ W, T* __restrict__ Q, int64_t ldq,
+                              int col, T* __restrict__ Z, T* __restrict__ Zs, const T* __restrict__ a) {
+  const int64_t tot = n * B;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < tot; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = t / B;
+    const int c = (int)(t % B);
+    const T v = W[t];
+    if (Q) Q[i * ldq + col + c] = v;
+    if (Z) Z[t] = v;
+    if (Zs) Zs[t] = a[i] * v;
+  }
+}
+
+// H[m0:m0+B, m0:m0+B] = sym(C1 + C2 rows m0..m0+B); coupling R = R2 R1 into
+// H[m0+B:m0+2B, m0:m0+B] and its transpose.
+__global__ void hblock_kernel(int B, double* __restrict__ H, int64_t ldh, int m0, const double* __restrict__ C1,
+                              const double* __restrict__ C2, const double* __restrict__ R1,
+                              const double* __restrict__ R2, double* __restrict__ Rout, int write_coupling) {
+  const int r = threadIdx.y, c = threadIdx.x;
+  if (r >= B || c >= B) return;
+  const double d1 = C1[(int64_t)(m0 + r) * B + c] + (C2 ? C2[(int64_t)(m0 + r) * B + c] : 0.0);
+  const double d2 = C1[(int64_t)(m0 + c) * B + r] + (C2 ? C2[(int64_t)(m0 + c) * B + r] : 0.0);
+  H[(int64_t)(m0 + r) * ldh + m0 + c] = 0.5 * (d1 + d2);
+  // R = R2 R1 (both upper triangular)
+  double s = 0.0;
+  for (int k = 0; k < B; ++k) s += R2[r * B + k] * R1[k * B + c];
+  if (Rout) Rout[r * B + c] = s;
+  if (write_coupling) {
+    H[(int64_t)(m0 + B + r) * ldh + m0 + c] = s;
+    H[(int64_t)(m0 + c) * ldh + m0 + B + r] = s;
+  }
+}
+
+// out[i, 0:k] = Q[i, 0:m] Y[0:m, 0:k]   (warp per row, lane = output column
+// inside a 32-column tile given by blockIdx.y)
+template <typename TQ, typename TA, typename TO>
+__global__ void __launch_bounds__(256)
+rotate_kernel(int64_t n, const TQ* __restrict__ Q, int64_t ldq, int m, const double* __restrict__ Y,
+              int64_t ldy, int k, TO* __restrict__ out, int64_t ldo) {
+  extern __shared__ __align__(16) unsigned char sraw[];
+  TA* ys = reinterpret_cast<TA*>(sraw);  // m x 32
+  const int q0 = blockIdx.y * 32;
+  for (int t = threadIdx.x; t < m * 32; t += blockDim.x) {
+    const int p = t / 32, q = t % 32;
+    ys[t] = (q0 + q < k) ? (TA)Y[(int64_t)p * ldy + q0 + q] : TA(0);
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t i = gw; i < n; i += nw) {
+    TA acc = TA(0);
+    for (int p0 = 0; p0 < m; p0 += 32) {
+      const TA qv = (p0 + lane < m) ? (TA)Q[i * ldq + p0 + lane] : TA(0);
+      const int lim = min(32, m - p0);
+      for (int t = 0; t < lim; ++t) acc = fma(__shfl_sync(0xffffffffu, qv, t), ys[(p0 + t) * 32 + lane], acc);
+    }
+    if (q0 + lane < k) out[i * ldo + q0 + lane] = (TO)acc;
+  }
+}
+
+// Uniform [-0.5, 0.5) values from a splitmix64 hash of (seed, index):
+// deterministic and identical on every platform.
+__device__ __forceinline__ uint64_t splitmix64(uint64_t x) {
+  x += 0x9e3779b97f4a7c15ull;
+  x = (x ^ (x >> 30)) * 0xbf58476d1ce4e5b9ull;
+  x = (x ^ (x >> 27)) * 0x94d049bb133111ebull;
+  return x ^ (x >> 31);
+}
+
+template <typename T>
+__global__ void fill_random(int64_t count, uint64_t seed, T* __restrict__ out) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < count; t += (int64_t)gridDim.x * blockDim.x) {
+    const uint64_t h = splitmix64(seed * 0x2545f4914f6cdd1dull + (uint64_t)t);
+    out[t] = (T)((double)(h >> 11) * (1.0 / 9007199254740992.0) - 0.5);
+  }
+}
+
+template <typename T, int B>
+int proj_t(int64_t n, const T* Q, int64_t ldq, int ncols, const T* W, double* part, int nparts, double* C,
+           cudaStream_t s) {
+  if (ncols <= kProjBlock) proj_partial<T, B, 1><<<nparts, kProjBlock, 0, s>>>(n, Q, ldq, ncols, W, part);
+  else if (ncols <= 2 * kProjBlock) proj_partial<T, B, 2><<<nparts, kProjBlock, 0, s>>>(n, Q, ldq, ncols, W, part);
+  else if (ncols <= 4 * kProjBlock && B <= 8) proj_partial<T, B <= 8 ? B : 8, 4><<<nparts, kProjBlock, 0, s>>>(n, Q, ldq, ncols, W, part);
+  else return SG_ERR_ARG;
+  SG_CHECK_LAUNCH();
+  const int tot = ncols * B;
+  proj_reduce<<<(tot + 255) / 256, 256, 0, s>>>(nparts, ncols, B, part, C);
+  SG_CHECK_LAUNCH();
+  return SG_OK;
+}
+
+template <typename T>
+int proj_dispatch(int B, int64_t n, const T* Q, int64_t ldq, int ncols, const T* W, double* part, int nparts,
+                  double* C, cudaStream_t s) {
+  switch (B) {
+    case 4: return proj_t<T, 4>(n, Q, ldq, ncols, W, part, nparts, C, s);
+    case 8: return proj_t<T, 8>(n, Q, ldq, ncols, W, part, nparts, C, s);
+    case 16: return proj_t<T, 16>(n, Q, ldq, ncols, W, part, nparts, C, s);
+    case 32: return proj_t<T, 32>(n, Q, ldq, ncols, W, part, nparts, C, s);
+    default: return SG_ERR_ARG;
+  }
+}
+
+template <typename T>
+int update_dispatch(int B, int64_t n, const T* Q, int64_t ldq, int ncols, const double* C, T* W, cudaStream_t s) {
+  const int grid = grid_for(n * 32, 256, 8 * sm_count_l());
+  const size_t smem = (size_t)ncols * B * sizeof(T);
+  if (smem > 200 * 1024) return SG_ERR_ARG;
+#define SG_UPD(BB)                                                                                   \
+  case BB:                                                                                           \
+    if (smem > 48 * 1024 &&                                                                          \
+        cudaFuncSetAttribute(update_kernel<T, BB>, cudaFuncAttributeMaxDynamicSharedMemorySize,      \
+                             (int)smem) != cudaSuccess)                                              \
+      return SG_ERR_CUDA;                                                                            \
+    update_kernel<T, BB><<<grid, 256, smem, s>>>(n, Q, ldq, ncols, C, W);                            \
+    break;
+  switch (B) {
+    SG_UPD(4) SG_UPD(8) SG_UPD(16) SG_UPD(32)
+    default: return SG_ERR_ARG;
+  }
+#undef SG_UPD
+  SG_CHECK_LAUNCH();
+  return SG_OK;
+}
+
+template <typename T>
+int rinv_dispatch(int B, int64_t n, const double* Rinv, T* W, cudaStream_t s) {
+  const int grid = grid_for(n * 32, 256, 8 * sm_count_l());
+  switch (B) {
+    case 4: apply_rinv<T, 4><<<grid, 256, 0, s>>>(n, Rinv, W); break;
+    case 8: apply_rinv<T, 8><<<grid, 256, 0, s>>>(n, Rinv, W); break;
+    case 16: apply_rinv<T, 16><<<grid, 256, 0, s>>>(n, Rinv, W); break;
+    case 32: apply_rinv<T, 32><<<grid, 256, 0, s>>>(n, Rinv, W); break;
+    default: return SG_ERR_ARG;
+  }
+  SG_CHECK_LAUNCH();
+  return SG_OK;
+}
+
+}  // namespace
+}  // namespace sg
+
+using namespace sg;
+
+extern "C" int sg_proj_parts(void) { return 2 * sm_count_l(); }
+
+extern "C" int sg_fill_random(int dtype, int64_t count, uint64_t seed, void* out, void* stream) {
+  if (count < 0) return SG_ERR_ARG;
+  if (count == 0) return SG_OK;
+  cudaStream_t s = as_stream(stream);
+  const int grid = grid_for(count, 256, 16 * sm_count_l());
+  if (dtype == 0) fill_random<float><<<grid, 256, 0, s>>>(count, seed, (float*)out);
+  else if (dtype == 1) fill_random<double><<<grid, 256, 0, s>>>(count, seed, (double*)out);
+  else return SG_ERR_ARG;
+  SG_CHECK_LAUNCH();
+  return SG_OK;
+}
+
+extern "C" int sg_block_proj(int dtype, int block, int64_t n, const void* Q, int64_t ldq, int ncols,
+                             const void* W, double* part, int nparts, double* C, void* stream) {
+  if (n <= 0 || ncols <= 0 || nparts <= 0) return SG_ERR_ARG;
+  cudaStream_t s = as_stream(stream);
+  if (dtype == 0) return proj_dispatch<float>(block, n, (const float*)Q, ldq, ncols, (const float*)W, part, nparts, C, s);
+  if (dtype == 1) return proj_dispatch<double>(block, n, (const double*)Q, ldq, ncols, (const double*)W, part, nparts, C, s);
+  return SG_ERR_ARG;
+}
+
+extern "C" int sg_block_update(int dtype, int block, int64_t n, const void* Q, int64_t ldq, int ncols,
+                               const double* C, void* W, void* stream) {
+  if (n <= 0 || ncols <= 0) return SG_ERR_ARG;
+  cudaStream_t s = as_stream(stream);
+  if (dtype == 0) return update_dispatch<float>(block, n, (const float*)Q, ldq, ncols, C, (float*)W, s);
+  if (dtype == 1) return update_dispatch<double>(block, n, (const double*)Q, ldq, ncols, C, (double*)W, s);
+  return SG_ERR_ARG;
+}
+
+// One Cholesky-QR pass: G = WᵀW, G = RᵀR, W <- W R⁻¹.  G, R, Rinv: B x B FP64.
+extern "C" int sg_block_cholqr(int dtype, int block, int64_t n, void* W, double* part, int nparts, double* G,
+                               double* R, double* Rinv, int* status, void* stream) {
+  if (n <= 0 || block < 1 || block > 32) return SG_ERR_ARG;
+  int e = sg_block_proj(dtype, block, n, W, block, block, W, part, nparts, G, stream);
+  if (e) return e;
+  cudaStream_t s = as_stream(stream);
+  chol_kernel<<<1, 32, 0, s>>>(block, G, R, Rinv, status);
+  SG_CHECK_LAUNCH();
+  if (dtype == 0) return rinv_dispatch<float>(block, n, Rinv, (float*)W, s);
+  if (dtype == 1) return rinv_dispatch<double>(block, n, Rinv, (double*)W, s);
+  return SG_ERR_ARG;
+}
+
+extern "C" int sg_block_finish(int dtype, int block, int64_t n, const void* W, void* Q, int64_t ldq, int col,
+                               void* Z, void* Zs, const void* rowscale, void* stream) {
+  if (n <= 0 || (Zs && !rowscale)) return SG_ERR_ARG;
+  cudaStream_t s = as_stream(stream);
+  const int grid = grid_for(n * block, 256, 16 * sm_count_l());
+  if (dtype == 0)
+    finish_kernel<float><<<grid, 256, 0, s>>>(n, block, (const float*)W, (float*)Q, ldq, col, (float*)Z,
+                                              (float*)Zs, (const float*)rowscale);
+  else if (dtype == 1)
+    finish_kernel<double><<<grid, 256, 0, s>>>(n, block, (const double*)W, (double*)Q, ldq, col, (double*)Z,
+                                               (double*)Zs, (const double*)rowscale);
+  else
+    return SG_ERR_ARG;
+  SG_CHECK_LAUNCH();
+  return SG_OK;
+}
+
+extern "C" int sg_lanczos_hblock(int block, double* H, int64_t ldh, int m0, const double* C1, const double* C2,
+                                 const double* R1, const double* R2, double* Rout, int write_coupling,
+                                 void* stream) {
+  if (block < 1 || block > 32 || m0 < 0) return SG_ERR_ARG;
+  hblock_kernel<<<1, dim3(block, block), 0, as_stream(stream)>>>(block, H, ldh, m0, C1, C2, R1, R2, Rout,
+                                                                 write_coupling);
+  SG_CHECK_LAUNCH();
+  return SG_OK;
+}
+
+// out[:, 0:k] = Q[:, 0:m] Y[0:m, 0:k].  tq/to: 0 = float, 1 = double (the
+// accumulation runs in the wider of the two).
+extern "C" int sg_basis_rotate(int tq, int to, int64_t n, const void* Q, int64_t ldq, int m, const double* Y,
+                               int64_t ldy, int k, void* out, int64_t ldo, void* stream) {
+  if (n <= 0 || m <= 0 || k <= 0 || m > 1536) return SG_ERR_ARG;
+  cudaStream_t s = as_stream(stream);
+  const int gx = grid_for(n * 32, 256, 8 * sm_count_l());
+  dim3 grid(gx, (k + 31) / 32);
+  const bool wide = tq == 1 || to == 1;
+  const size_t smem = (size_t)m * 32 * (wide ? sizeof(double) : sizeof(float));
+  if (smem > 200 * 1024) return SG_ERR_ARG;
+#define SG_ROT(TQ, TA, TO)                                                                              \
+  do {                                                                                                  \
+    if (smem > 48 * 1024 &&                                                                             \
+        cudaFuncSetAttribute(rotate_kernel<TQ, TA, TO>, cudaFuncAttributeMaxDynamicSharedMemorySize,    \
+                             (int)smem) != cudaSuccess)                                                 \
+      return SG_ERR_CUDA;                                                                               \
+    rotate_kernel<TQ, TA, TO><<<grid, 256, smem, s>>>(n, (const TQ*)Q, ldq, m, Y, ldy, k, (TO*)out, ldo); \
+  } while (0)
+  if (tq == 0 && to == 0) SG_ROT(float, float, float);
+  else if (tq == 0 && to == 1) SG_ROT(float, double, double);
+  else if (tq == 1 && to == 1) SG_ROT(double, double, double);
+  else if (tq == 1 && to == 0) SG_ROT(double, double, float);
+  else return SG_ERR_ARG;
+#undef SG_ROT
+  SG_CHECK_LAUNCH();
+  return SG_OK;
+}

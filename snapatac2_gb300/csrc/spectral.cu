@@ -1,0 +1,490 @@
+// Matrix-free cosine spectral operator: feature selection, deterministic CSR
+// transpose, IDF weights, row normalisation, degree, and the two CSR SpMM
+// kernels of the Gram product.
+//
+// Reference arithmetic (snapatac2-python/src/embedding.rs):
+//   idf        269-286   w_j = ln(n / c_j), c_j = nnz of column j (0 -> 1,
+//                        n -> n-1; all counts equal -> w = 1)
+//   normalize  315-326   Xn = diag(1/||(XW)_i||) X W
+//   degree     139-152   colsum = 1ᵀXn, d = Xn colsum, D⁻¹ = 1/(d - 1)
+//   eigen      155-171   operator v -> X̂ (X̂ᵀ v) - D⁻¹ v, X̂ = diag(sqrt(D⁻¹)) Xn
+// With a_i = sqrt(D⁻¹_i)/||(XW)_i|| the operator is
+//   A v = a ⊙ (X (w² ⊙ (Xᵀ (a ⊙ v)))) - D⁻¹ ⊙ v
+// so X is kept as an index-only pattern (or with its integer counts) and the
+// scalings are folded into the SpMM prologue/epilogue.
+#include "common.cuh"
+#include "internal.h"
+
+namespace sg {
+namespace {
+
+// ---------------------------------------------------------------------------
+// column selection: keep entries whose column maps to >= 0, renumbered
+// ---------------------------------------------------------------------------
+__global__ void select_count(int64_t n, const int64_t* __restrict__ ptr, const int32_t* __restrict__ idx,
+                             const int32_t* __restrict__ colmap, int64_t* __restrict__ cnt) {
+  const int lane = threadIdx.x & 31;
+  const int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t r = w; r < n; r += nw) {
+    int64_t c = 0;
+    for (int64_t e = ptr[r] + lane; e < ptr[r + 1]; e += 32) c += colmap[idx[e]] >= 0;
+    for (int o = 16; o; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+    if (lane == 0) cnt[r + 1] = c;
+  }
+}
+
+__global__ void select_fill(int64_t n, const int64_t* __restrict__ ptr, const int32_t* __restrict__ idx,
+                            const float* __restrict__ val, const int32_t* __restrict__ colmap,
+                            const int64_t* __restrict__ optr, int32_t* __restrict__ oidx,
+                            float* __restrict__ oval) {
+  const int lane = threadIdx.x & 31;
+  const int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t r = w; r < n; r += nw) {
+    int64_t o = optr[r];
+    const int64_t b = ptr[r], e = ptr[r + 1];
+    for (int64_t k0 = b; k0 < e; k0 += 32) {
+      const int64_t k = k0 + lane;
+      int nc = -1;
+      if (k < e) nc = colmap[idx[k]];
+      const unsigned keep = __ballot_sync(0xffffffffu, nc >= 0);
+      if (nc >= 0) {
+        const int64_t p = o + __popc(keep & lanemask_lt());
+        oidx[p] = nc;
+        if (oval) oval[p] = val[k];
+      }
+      o += __popc(keep);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// deterministic transpose (CSR -> CSC) with rows ascending inside each column
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(512) tr_count(int64_t n, int64_t m, const int64_t* __restrict__ ptr,
+                                                const int32_t* __restrict__ idx, int nblk,
+                                                int32_t* __restrict__ cnt, int* status) {
+  const int b = blockIdx.x;
+  const int64_t r0 = n * b / nblk, r1 = n * (b + 1) / nblk;
+  int32_t* c = cnt + (int64_t)b * m;
+  for (int64_t r = r0; r < r1; ++r) {
+    const int64_t s = ptr[r], e = ptr[r + 1];
+    for (int64_t k = s + threadIdx.x; k < e; k += blockDim.x) {
+      const int j = idx[k];
+      if (j < 0 || j >= m || (k > s && idx[k - 1] >= j)) {  // need sorted, unique, in range
+        report_error(status, nullptr, SG_ERR_ARG, 0);
+        continue;
+      }
+      atomicAdd(c + j, 1);
+    }
+  }
+}
+
+// colptr[j+1] = total count of column j
+__global__ void tr_total(int64_t m, int nblk, const int32_t* __restrict__ cnt, int64_t* __restrict__ colptr) {
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < m; j += (int64_t)gridDim.x * blockDim.x) {
+    int64_t t = 0;
+    for (int b = 0; b < nblk; ++b) t += cnt[(int64_t)b * m + j];
+    colptr[j + 1] = t;
+    if (j == 0) colptr[0] = 0;
+  }
+}
+
+// cnt[b][j] <- colptr[j] + sum_{b' < b} cnt[b'][j]  (cursor of row block b)
+__global__ void tr_offsets(int64_t m, int nblk, int32_t* __restrict__ cnt, const int64_t* __restrict__ colptr,
+                           int64_t* __restrict__ cur) {
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < m; j += (int64_t)gridDim.x * blockDim.x) {
+    int64_t run = 0;
+    for (int b = 0; b < nblk; ++b) {
+      const int64_t c = cnt[(int64_t)b * m + j];
+      cnt[(int64_t)b * m + j] = (int32_t)run;  // offset inside the column
+      run += c;
+    }
+    (void)cur;
+  }
+}
+
+constexpr int kFillBlock = 512;
+constexpr int kFillItems = 8;
+
+__global__ void __launch_bounds__(kFillBlock)
+tr_fill(int64_t n, int64_t m, const int64_t* __restrict__ ptr, const int32_t* __restrict__ idx,
+        const float* __restrict__ val, int nblk, int32_t* __restrict__ cnt, const int64_t* __restrict__ colptr,
+        int32_t* __restrict__ rowidx, float* __restrict__ cval, int* status) {
+  if (*status) return;
+  const int b = blockIdx.x;
+  const int64_t r0 = n * b / nblk, r1 = n * (b + 1) / nblk;
+  int32_t* c = cnt + (int64_t)b * m;
+  for (int64_t r = r0; r < r1; ++r) {
+    const int64_t s = ptr[r], e = ptr[r + 1];
+    for (int64_t k0 = s; k0 < e; k0 += (int64_t)kFillBlock * kFillItems) {
+      int j[kFillItems];
+      int p[kFillItems];
+#pragma unroll
+      for (int t = 0; t < kFillItems; ++t) {
+        const int64_t k = k0 + (int64_t)t * kFillBlock + threadIdx.x;
+        j[t] = k < e ? idx[k] : -1;
+      }
+#pragma unroll
+      for (int t = 0; t < kFillItems; ++t) p[t] = j[t] >= 0 ? c[j[t]] : 0;
+#pragma unroll
+      for (int t = 0; t < kFillItems; ++t) {
+        if (j[t] >= 0) {
+          const int64_t k = k0 + (int64_t)t * kFillBlock + threadIdx.x;
+          c[j[t]] = p[t] + 1;
+          const int64_t dst = colptr[j[t]] + p[t];
+          rowidx[dst] = (int32_t)r;
+          if (cval) cval[dst] = val[k];
+        }
+      }
+    }
+    __syncthreads();  // the next row may touch the same columns
+  }
+}
+
+// ---------------------------------------------------------------------------
+// IDF weights, row norms, degree (FP64, as the reference)
+// ---------------------------------------------------------------------------
+__global__ void colcount_minmax(int64_t m, const int64_t* __restrict__ colptr, unsigned long long* mm) {
+  unsigned long long lo = ~0ull, hi = 0;
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < m; j += (int64_t)gridDim.x * blockDim.x) {
+    unsigned long long c = (unsigned long long)(colptr[j + 1] - colptr[j]);
+    lo = min(lo, c);
+    hi = max(hi, c);
+  }
+  for (int o = 16; o; o >>= 1) {
+    lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+    hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicMin(mm, lo);
+    atomicMax(mm + 1, hi);
+  }
+}
+
+__global__ void init_minmax(unsigned long long* mm) {
+  mm[0] = ~0ull;
+  mm[1] = 0ull;
+}
+
+__global__ void idf_kernel(int64_t n, int64_t m, const int64_t* __restrict__ colptr,
+                           const unsigned long long* __restrict__ mm, double* __restrict__ w) {
+  const bool equal = mm[0] == mm[1];
+  const double dn = (double)n;
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < m; j += (int64_t)gridDim.x * blockDim.x) {
+    if (equal) { w[j] = 1.0; continue; }
+    double c = (double)(colptr[j + 1] - colptr[j]);
+    if (c == 0.0) c = 1.0;
+    else if (c == dn) c = dn - 1.0;
+    w[j] = log(dn / c);
+  }
+}
+
+// rinv_i = 1 / ||(x_i ⊙ w)||_2
+__global__ void rownorm_kernel(int64_t n, const int64_t* __restrict__ ptr, const int32_t* __restrict__ idx,
+                               const float* __restrict__ val, const double* __restrict__ w,
+                               double* __restrict__ rinv, int* status, unsigned long long* bad) {
+  const int lane = threadIdx.x & 31;
+  const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t r = gw; r < n; r += nw) {
+    double s = 0.0;
+    for (int64_t k = ptr[r] + lane; k < ptr[r + 1]; k += 32) {
+      double x = w[idx[k]];
+      if (val) x *= (double)val[k];
+      s = fma(x, x, s);
+    }
+    for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) {
+      if (!(s > 0.0)) report_error(status, bad, SG_ERR_NUMERIC, (unsigned long long)r);
+      rinv[r] = 1.0 / sqrt(s);
+    }
+  }
+}
+
+// colsum_j = w_j * sum_{i in col j} x_ij rinv_i   (CSC gather)
+__global__ void colsum_kernel(int64_t m, const int64_t* __restrict__ cptr, const int32_t* __restrict__ ridx,
+                              const float* __restrict__ cval, const double* __restrict__ w,
+                              const double* __restrict__ rinv, double* __restrict__ colsum) {
+  const int lane = threadIdx.x & 31;
+  const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t j = gw; j < m; j += nw) {
+    double s = 0.0;
+    for (int64_t k = cptr[j] + lane; k < cptr[j + 1]; k += 32) {
+      double x = rinv[ridx[k]];
+      if (cval) x *= (double)cval[k];
+      s += x;
+    }
+    for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) colsum[j] = s * w[j];
+  }
+}
+
+// d_i = rinv_i * sum_j x_ij w_j colsum_j ; dinv = 1/(d-1) ; a = rinv*sqrt(dinv)
+__global__ void degree_kernel(int64_t n, const int64_t* __restrict__ ptr, const int32_t* __restrict__ idx,
+                              const float* __restrict__ val, const double* __restrict__ w,
+                              const double* __restrict__ colsum, const double* __restrict__ rinv,
+                              double* __restrict__ a, double* __restrict__ dinv, float* __restrict__ a32,
+                              float* __restrict__ dinv32, int* status, unsigned long long* bad) {
+  const int lane = threadIdx.x & 31;
+  const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t r = gw; r < n; r += nw) {
+    double s = 0.0;
+    for (int64_t k = ptr[r] + lane; k < ptr[r + 1]; k += 32) {
+      const int j = idx[k];
+      double x = w[j] * colsum[j];
+      if (val) x *= (double)val[k];
+      s += x;
+    }
+    for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) {
+      const double d = s * rinv[r];
+      const double di = 1.0 / (d - 1.0);
+      if (!(di > 0.0) || isinf(di)) report_error(status, bad, SG_ERR_NUMERIC, (unsigned long long)r);
+      const double ai = rinv[r] * sqrt(di);
+      a[r] = ai;
+      dinv[r] = di;
+      if (a32) a32[r] = (float)ai;
+      if (dinv32) dinv32[r] = (float)di;
+    }
+  }
+}
+
+__global__ void square_weights(int64_t m, const double* __restrict__ w, double* __restrict__ w2,
+                               float* __restrict__ w2f) {
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < m; j += (int64_t)gridDim.x * blockDim.x) {
+    const double v = w[j] * w[j];
+    w2[j] = v;
+    if (w2f) w2f[j] = (float)v;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// CSR SpMM over a block of B dense columns:
+//   out[r,:] = s_r * sum_{e in row r} x_e * in[col_e,:]  (- d_r * y[r,:])
+// One warp per row.  The B values of a gathered row are split into 16-byte
+// vectors, LPN lanes per nonzero, so each warp step gathers 32/LPN rows with
+// coalesced 128-bit loads; the 32 column indices of a chunk are read once
+// (one coalesced 128-byte load) and broadcast by shuffles.  Partial sums are
+// combined by a fixed xor-shuffle tree: results are deterministic.
+// ---------------------------------------------------------------------------
+template <typename T> struct V16;
+template <> struct V16<float> {
+  using type = float4;
+  static constexpr int n = 4;
+  __device__ static float4 zero() { return make_float4(0.f, 0.f, 0.f, 0.f); }
+  __device__ static void add(float4& a, const float4& b) { a.x += b.x; a.y += b.y; a.z += b.z; a.w += b.w; }
+  __device__ static void fma(float4& a, float s, const float4& b) {
+    a.x = fmaf(s, b.x, a.x); a.y = fmaf(s, b.y, a.y); a.z = fmaf(s, b.z, a.z); a.w = fmaf(s, b.w, a.w);
+  }
+  __device__ static float4 shfl_xor(const float4& v, int o) {
+    return make_float4(__shfl_xor_sync(0xffffffffu, v.x, o), __shfl_xor_sync(0xffffffffu, v.y, o),
+                       __shfl_xor_sync(0xffffffffu, v.z, o), __shfl_xor_sync(0xffffffffu, v.w, o));
+  }
+};
+template <> struct V16<double> {
+  using type = double2;
+  static constexpr int n = 2;
+  __device__ static double2 zero() { return make_double2(0.0, 0.0); }
+  __device__ static void add(double2& a, const double2& b) { a.x += b.x; a.y += b.y; }
+  __device__ static void fma(double2& a, double s, const double2& b) { a.x = ::fma(s, b.x, a.x); a.y = ::fma(s, b.y, a.y); }
+  __device__ static double2 shfl_xor(const double2& v, int o) {
+    return make_double2(__shfl_xor_sync(0xffffffffu, v.x, o), __shfl_xor_sync(0xffffffffu, v.y, o));
+  }
+};
+
+template <typename T, int B, bool VALUED, bool SHIFT>
+__global__ void __launch_bounds__(256)
+spmm_kernel(int64_t rows, const int64_t* __restrict__ ptr, const int32_t* __restrict__ idx,
+            const float* __restrict__ val, const T* __restrict__ in, T* __restrict__ out,
+            const T* __restrict__ scale, const T* __restrict__ dshift, const T* __restrict__ y) {
+  using VT = typename V16<T>::type;
+  constexpr int VW = V16<T>::n;
+  constexpr int LPN = B / VW;          // lanes per nonzero
+  constexpr int NPS = 32 / LPN;        // nonzeros per warp step
+  constexpr int CH = LPN >= 4 ? 1 : 4 / LPN;  // 32-index chunks per iteration
+  static_assert(B % VW == 0 && LPN >= 1 && LPN <= 32, "unsupported block width");
+  const int lane = threadIdx.x & 31;
+  const int sub = lane % LPN, slot = lane / LPN;
+  const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t r = gw; r < rows; r += nw) {
+    const int64_t s = ptr[r], e = ptr[r + 1];
+    VT acc = V16<T>::zero();
+    for (int64_t base = s; base < e; base += 32 * CH) {
+      int ci[CH];
+      float cv[CH];
+#pragma unroll
+      for (int c = 0; c < CH; ++c) {
+        const int64_t k = base + c * 32 + lane;
+        ci[c] = k < e ? __ldg(idx + k) : -1;
+        cv[c] = (VALUED && k < e) ? __ldg(val + k) : 1.0f;
+      }
+      VT g[CH * LPN];
+      int gc[CH * LPN];
+      float gv[CH * LPN];
+#pragma unroll
+      for (int c = 0; c < CH; ++c)
+#pragma unroll
+        for (int j = 0; j < LPN; ++j) {
+          const int col = __shfl_sync(0xffffffffu, ci[c], j * NPS + slot);
+          gc[c * LPN + j] = col;
+          if (VALUED) gv[c * LPN + j] = __shfl_sync(0xffffffffu, cv[c], j * NPS + slot);
+          g[c * LPN + j] = col >= 0 ? __ldg(reinterpret_cast<const VT*>(in + (int64_t)col * B) + sub)
+                                    : V16<T>::zero();
+        }
+#pragma unroll
+      for (int t = 0; t < CH * LPN; ++t) {
+        if (VALUED) V16<T>::fma(acc, (T)gv[t], g[t]);
+        else V16<T>::add(acc, g[t]);
+      }
+    }
+#pragma unroll
+    for (int o = LPN; o < 32; o <<= 1) V16<T>::add(acc, V16<T>::shfl_xor(acc, o));
+    if (slot == 0) {
+      const T sc = scale[r];
+      T* op = out + r * B + sub * VW;
+      const T* a = reinterpret_cast<const T*>(&acc);
+      if (SHIFT) {
+        const T d = dshift[r];
+        const T* yp = y + r * B + sub * VW;
+        VT o;
+        T* ov = reinterpret_cast<T*>(&o);
+#pragma unroll
+        for (int q = 0; q < VW; ++q) ov[q] = sc * a[q] - d * yp[q];
+        *reinterpret_cast<VT*>(op) = o;
+      } else {
+        VT o;
+        T* ov = reinterpret_cast<T*>(&o);
+#pragma unroll
+        for (int q = 0; q < VW; ++q) ov[q] = sc * a[q];
+        *reinterpret_cast<VT*>(op) = o;
+      }
+    }
+  }
+}
+
+template <typename T, int B>
+int launch_spmm_t(int64_t rows, const int64_t* ptr, const int32_t* idx, const float* val, const T* in,
+                  T* out, const T* scale, const T* dshift, const T* y, int grid, cudaStream_t s) {
+  if (val) {
+    if (dshift) spmm_kernel<T, B, true, true><<<grid, 256, 0, s>>>(rows, ptr, idx, val, in, out, scale, dshift, y);
+    else spmm_kernel<T, B, true, false><<<grid, 256, 0, s>>>(rows, ptr, idx, val, in, out, scale, dshift, y);
+  } else {
+    if (dshift) spmm_kernel<T, B, false, true><<<grid, 256, 0, s>>>(rows, ptr, idx, val, in, out, scale, dshift, y);
+    else spmm_kernel<T, B, false, false><<<grid, 256, 0, s>>>(rows, ptr, idx, val, in, out, scale, dshift, y);
+  }
+  return cudaGetLastError() == cudaSuccess ? SG_OK : SG_ERR_CUDA;
+}
+
+template <typename T>
+int launch_spmm(int B, int64_t rows, const int64_t* ptr, const int32_t* idx, const float* val, const T* in,
+                T* out, const T* scale, const T* dshift, const T* y, int grid, cudaStream_t s) {
+  switch (B) {
+    case 4: return launch_spmm_t<T, 4>(rows, ptr, idx, val, in, out, scale, dshift, y, grid, s);
+    case 8: return launch_spmm_t<T, 8>(rows, ptr, idx, val, in, out, scale, dshift, y, grid, s);
+    case 16: return launch_spmm_t<T, 16>(rows, ptr, idx, val, in, out, scale, dshift, y, grid, s);
+    case 32: return launch_spmm_t<T, 32>(rows, ptr, idx, val, in, out, scale, dshift, y, grid, s);
+    default: return SG_ERR_ARG;
+  }
+}
+
+int sm_count() {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  return sms > 0 ? sms : 1;
+}
+
+}  // namespace
+}  // namespace sg
+
+using namespace sg;
+
+extern "C" int sg_csr_select_cols(int64_t n, const int64_t* indptr, const int32_t* indices, const float* values,
+                                  const int32_t* colmap, int64_t* out_indptr, int32_t* out_indices,
+                                  float* out_values, void* scan_scratch, void* stream) {
+  if (n < 0) return SG_ERR_ARG;
+  cudaStream_t s = as_stream(stream);
+  if (n == 0) return cudaMemsetAsync(out_indptr, 0, sizeof(int64_t), s) == cudaSuccess ? SG_OK : SG_ERR_CUDA;
+  const int grid = grid_for(n * 32, 256, 8 * sm_count() * 8);
+  if (cudaMemsetAsync(out_indptr, 0, sizeof(int64_t), s) != cudaSuccess) return SG_ERR_CUDA;
+  select_count<<<grid, 256, 0, s>>>(n, indptr, indices, colmap, out_indptr);
+  SG_CHECK_LAUNCH();
+  if (inclusive_scan_i64(out_indptr + 1, n, scan_scratch, s) != cudaSuccess) return SG_ERR_CUDA;
+  select_fill<<<grid, 256, 0, s>>>(n, indptr, indices, values, colmap, out_indptr, out_indices, out_values);
+  SG_CHECK_LAUNCH();
+  return SG_OK;
+}
+
+extern "C" int sg_transpose_blocks(void) { return 2 * sm_count(); }
+
+extern "C" int sg_csr_transpose(int64_t n, int64_t m, const int64_t* indptr, const int32_t* indices,
+                                const float* values, int nblk, int32_t* work, int64_t* colptr,
+                                int32_t* rowidx, float* cvalues, void* scan_scratch, int* status,
+                                void* stream) {
+  if (n < 0 || m <= 0 || nblk <= 0 || m > 0x7fffffffLL || n > 0x7fffffffLL) return SG_ERR_ARG;
+  cudaStream_t s = as_stream(stream);
+  if (cudaMemsetAsync(work, 0, (size_t)nblk * (size_t)m * sizeof(int32_t), s) != cudaSuccess) return SG_ERR_CUDA;
+  tr_count<<<nblk, 512, 0, s>>>(n, m, indptr, indices, nblk, work, status);
+  SG_CHECK_LAUNCH();
+  const int g = grid_for(m, 256, 4096);
+  tr_total<<<g, 256, 0, s>>>(m, nblk, work, colptr);
+  SG_CHECK_LAUNCH();
+  if (inclusive_scan_i64(colptr + 1, m, scan_scratch, s) != cudaSuccess) return SG_ERR_CUDA;
+  tr_offsets<<<g, 256, 0, s>>>(m, nblk, work, colptr, nullptr);
+  SG_CHECK_LAUNCH();
+  tr_fill<<<nblk, kFillBlock, 0, s>>>(n, m, indptr, indices, values, nblk, work, colptr, rowidx, cvalues, status);
+  SG_CHECK_LAUNCH();
+  return SG_OK;
+}
+
+extern "C" int sg_spectral_prepare(int64_t n, int64_t m, const int64_t* indptr, const int32_t* indices,
+                                   const float* values, const int64_t* colptr, const int32_t* rowidx,
+                                   const float* cvalues, const double* feature_weights, double* w,
+                                   double* w2, float* w2_32, double* rinv, double* colsum, double* a,
+                                   double* dinv, float* a32, float* dinv32, unsigned long long* minmax,
+                                   int* status, unsigned long long* bad, void* stream) {
+  if (n <= 0 || m <= 0) return SG_ERR_ARG;
+  cudaStream_t s = as_stream(stream);
+  const int sms = sm_count();
+  const int gm = grid_for(m, 256, 8 * sms);
+  const int gw_rows = grid_for(n * 32, 256, 8 * sms * 4);
+  const int gw_cols = grid_for(m * 32, 256, 8 * sms * 4);
+  if (feature_weights) {
+    if (cudaMemcpyAsync(w, feature_weights, (size_t)m * sizeof(double), cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+      return SG_ERR_CUDA;
+  } else {
+    init_minmax<<<1, 1, 0, s>>>(minmax);
+    colcount_minmax<<<gm, 256, 0, s>>>(m, colptr, minmax);
+    SG_CHECK_LAUNCH();
+    idf_kernel<<<gm, 256, 0, s>>>(n, m, colptr, minmax, w);
+    SG_CHECK_LAUNCH();
+  }
+  square_weights<<<gm, 256, 0, s>>>(m, w, w2, w2_32);
+  rownorm_kernel<<<gw_rows, 256, 0, s>>>(n, indptr, indices, values, w, rinv, status, bad);
+  colsum_kernel<<<gw_cols, 256, 0, s>>>(m, colptr, rowidx, cvalues, w, rinv, colsum);
+  degree_kernel<<<gw_rows, 256, 0, s>>>(n, indptr, indices, values, w, colsum, rinv, a, dinv, a32, dinv32,
+                                        status, bad);
+  SG_CHECK_LAUNCH();
+  return SG_OK;
+}
+
+extern "C" int sg_spmm(int dtype, int block, int64_t rows, const int64_t* ptr, const int32_t* idx,
+                       const float* val, const void* in, void* out, const void* scale, const void* dshift,
+                       const void* y, int grid, void* stream) {
+  if (rows < 0 || !scale || (dshift && !y)) return SG_ERR_ARG;
+  if (rows == 0) return SG_OK;
+  if (grid <= 0) grid = grid_for(rows * 32, 256, 8 * sm_count() * 4);
+  cudaStream_t s = as_stream(stream);
+  if (dtype == 0)
+    return launch_spmm<float>(block, rows, ptr, idx, val, (const float*)in, (float*)out, (const float*)scale,
+                              (const float*)dshift, (const float*)y, grid, s);
+  if (dtype == 1)
+    return launch_spmm<double>(block, rows, ptr, idx, val, (const double*)in, (double*)out,
+                               (const double*)scale, (const double*)dshift, (const double*)y, grid, s);
+  return SG_ERR_ARG;
+}

@@ -168,8 +168,9 @@ run_kernel(const int64_t* __restrict__ cell_ptr, int64_t n_cells, int64_t n_frag
         A[o] = lo;
         if (r == 2) A[o + 1] = hi;
       }
-      kmin = min(kmin, lo);
-      kmax = max(kmax, hi);
+      // a zero-length fragment has hi = lo - 1 (end = start - 1)
+      kmin = min(kmin, min(lo, hi));
+      kmax = max(kmax, max(lo, hi));
     }
   }
   __syncthreads();

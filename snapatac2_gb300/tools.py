@@ -1,0 +1,122 @@
+"""``snap.tl.spectral`` -- matrix-free cosine spectral embedding on the GPU.
+
+Drop-in counterpart of ``snapatac2-python/python/snapatac2/tools/_embedding.py:129-295``
+for ``distance_metric='cosine'`` with the full sample (``sample_size=None``):
+same keywords, defaults, ``n_comps`` clamp, ``weighted_by_sd`` post-processing,
+and output slots ``uns['spectral_eigenvalue']`` (float64[k']) and
+``obsm['X_spectral']`` (float64[n, k']).
+"""
+from __future__ import annotations
+
+from typing import Literal
+
+import numpy as np
+import scipy.sparse as sp
+import torch
+
+from . import _eigen
+from ._binning import DeviceCSR
+
+
+def _device(device=None) -> torch.device:
+    if device is not None:
+        return torch.device(device)
+    if not torch.cuda.is_available():
+        raise RuntimeError("snapatac2_gb300 needs a CUDA GPU (sm_103a); none is available")
+    return torch.device("cuda", torch.cuda.current_device())
+
+
+def csr_to_device(X, device) -> DeviceCSR:
+    """Upload a scipy CSR matrix (values kept only when not all equal to 1)."""
+    X = sp.csr_matrix(X)
+    if not X.has_sorted_indices:
+        X = X.copy()
+        X.sort_indices()
+    data = X.data
+    binary = data.size == 0 or bool(np.all(data == 1))
+    ip = torch.from_numpy(X.indptr.astype(np.int64, copy=False)).to(device, non_blocking=True)
+    ix = torch.from_numpy(X.indices.astype(np.int32, copy=False)).to(device, non_blocking=True)
+    val = None
+    if not binary:
+        if np.any(np.abs(data) >= 2 ** 24) and np.issubdtype(data.dtype, np.integer):
+            raise ValueError("count values of 2^24 or more do not fit the float32 value path")
+        val = torch.from_numpy(data.astype(np.float32)).to(device, non_blocking=True)
+    return DeviceCSR(ip, ix, val, X.shape)
+
+
+def spectral_embedding(X, features=None, n_comps: int = 30, random_state: int = 0, feature_weights=None, *,
+                       precision: str = "mixed", block: int = 8, device=None, return_info: bool = False,
+                       **solver_kw):
+    """(evals, evecs) of the normalised cosine operator, like the PyO3
+    ``spectral_embedding`` (``snapatac2-python/src/embedding.rs:24-59``):
+    top ``n_comps`` by magnitude, sorted descending; evecs float64 (n, k).
+
+    ``X`` is a scipy CSR matrix or a ``DeviceCSR`` already on the GPU.
+    """
+    dev = _device(device)
+    csr = X if isinstance(X, DeviceCSR) else csr_to_device(X, dev)
+    csr = _eigen.select_columns(csr, features)
+    op = _eigen.build_operator(csr, feature_weights)
+    res = _eigen.eigsh_lm(op, n_comps, precision=precision, block=block, seed=random_state, **solver_kw)
+    if return_info:
+        return res.evals, res.evecs, res.info
+    return res.evals, res.evecs.cpu().numpy()
+
+
+def spectral(
+    adata,
+    n_comps: int = 30,
+    features: str | np.ndarray | None = "selected",
+    random_state: int = 0,
+    sample_size: int | float | None = None,
+    sample_method: Literal["random", "degree"] = "random",
+    chunk_size: int = 20000,
+    distance_metric: Literal["jaccard", "cosine"] = "cosine",
+    weighted_by_sd: bool = True,
+    feature_weights: list[float] | None = None,
+    inplace: bool = True,
+    *,
+    precision: Literal["mixed", "fp64"] = "mixed",
+    block: int = 8,
+    device=None,
+):
+    """Laplacian-eigenmap embedding (``_embedding.py:129-295``), cosine, full sample.
+
+    Extra keywords: ``precision`` ('mixed': FP32 SpMM and basis with FP64
+    Rayleigh-Ritz; 'fp64': all FP64), ``block`` (Lanczos block size),
+    ``device``.
+    """
+    np.random.seed(random_state)
+    if isinstance(features, str):
+        if features in adata.var:
+            features = np.asarray(adata.var[features])
+        else:
+            raise NameError("Please call `select_features` first or explicitly set `features = None`")
+    n_comps = min(adata.n_vars - 1, adata.n_obs - 1, n_comps)
+    n_sample = adata.shape[0]
+    if sample_size is None:
+        sample_size = n_sample
+    elif isinstance(sample_size, int):
+        if sample_size <= 1:
+            raise ValueError("when sample_size is an integer, it should be > 1")
+        sample_size = min(sample_size, n_sample)
+    else:
+        if sample_size <= 0.0 or sample_size > 1.0:
+            raise ValueError("when sample_size is a float, it should be > 0 and <= 1")
+        sample_size = int(sample_size * n_sample)
+    if sample_size < n_sample:
+        raise NotImplementedError("Nyström sampling (sample_size < n_obs) is not supported")
+    if distance_metric != "cosine":
+        raise NotImplementedError("only distance_metric='cosine' (matrix-free) is supported")
+
+    evals, evecs = spectral_embedding(adata.X, features, n_comps, random_state, feature_weights,
+                                      precision=precision, block=block, device=device)
+    if weighted_by_sd:
+        idx = [i for i in range(evals.shape[0]) if evals[i] > 0]
+        evals = evals[idx]
+        evecs = evecs[:, idx] * np.sqrt(evals)
+    if inplace:
+        adata.uns["spectral_eigenvalue"] = evals
+        adata.obsm["X_spectral"] = evecs
+        return None
+    return evals, evecs
