@@ -1,0 +1,349 @@
+#!/usr/bin/env python
+"""Benchmark of the cell-embedding hot path: spectral cells/s at 30 components.
+
+Workload (one "step"): the matrix-free cosine spectral embedding (IDF
+weights, row normalisation, degree, block Krylov-Schur eigensolve of the
+top 30 eigenpairs by magnitude) of a synthetic 100,000-cell x 500,000-feature
+binary CSR with ~4,000 nonzeros per cell (cluster/Zipf model of the
+reference's workloads), mixed precision (FP32 SpMM and basis, FP64
+Rayleigh-Ritz).  ``value`` = cells/s with the CSR resident in HBM; ``e2e`` =
+the same through ``snapatac2_gb300.tl.spectral`` with the CSR in pinned host
+memory (host->device copy and the device->host read of X_spectral inside the
+timed region).  The all-FP64 GPU form is timed beside it and the mixed
+result is compared with it (eigenvalue relative error, principal angles).
+
+``--impl reference`` times the reference's own CPU arithmetic (IDF,
+normalisation, degree and SciPy ARPACK eigsh, restated in ``oracle/``) on a
+bounded sample of the same generator.
+
+Multi-GPU (torchrun, N > 1): the path is embedded independently per dataset
+("replicas only"): every rank embeds its own dataset; no collective touches
+the data path.
+"""
+from __future__ import annotations
+
+import argparse
+import csv
+import io
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "spectral cells/s @30 comps (mixed precision; FP64 GPU form and SpMM HBM GB/s reported beside)"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--cells", type=int, default=100_000)
+    p.add_argument("--features", type=int, default=500_000)
+    p.add_argument("--nnz", type=float, default=4000.0)
+    p.add_argument("--ncomps", type=int, default=30)
+    p.add_argument("--block", type=int, default=8)
+    p.add_argument("--fp64-steps", type=int, default=1)
+    p.add_argument("--e2e-steps", type=int, default=2)
+    p.add_argument("--cpu-sample-cells", type=int, default=2000)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+# --------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:  # noqa: BLE001 - clocks are best effort
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:  # noqa: BLE001
+            self.proc.kill()
+        self.f.close()
+        rows = list(csv.reader(io.StringIO(open(self.path).read())))
+        os.unlink(self.path)
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            r = [x.strip() for x in r]
+            if len(r) < 9:
+                continue
+            try:
+                sm.append(float(r[1]))
+                mx = float(r[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, r[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+class LaunchCounter:
+    """Counts kernels launched through the C ABI (calls x kernels per call)."""
+
+    def __init__(self):
+        from snapatac2_gb300 import _lib
+        self.lib = _lib.load()
+        self.table = _lib.KERNELS_PER_CALL
+        self.count = 0
+        self.active = False
+        for name in self.table:
+            fn = getattr(self.lib, name)
+
+            def wrap(*a, _fn=fn, _k=self.table[name]):
+                if self.active:
+                    self.count += _k
+                return _fn(*a)
+            setattr(self.lib, name, wrap)
+
+
+def peaks():
+    try:
+        d = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:  # noqa: BLE001
+        return 6800.0, "fallback"
+
+
+# --------------------------------------------------------------------------
+def cpu_reference_sample(n_cells: int, args, seed: int):
+    """The reference's arithmetic (oracle restatement, SciPy ARPACK) on a
+    sample of the same generator; returns (seconds, n_cells)."""
+    import scipy.sparse as sp
+    from oracle import spectral as osp
+    from snapatac2_gb300 import synthetic as syn
+    B = syn.binary_csr(n_cells, args.features, nnz_per_cell=args.nnz, seed=seed)
+    X = sp.csr_matrix((np.ones(B.nnz), B.indices, B.indptr), shape=B.shape)
+    t = time.perf_counter()
+    osp.spectral(X, n_comps=args.ncomps, random_state=0)
+    return time.perf_counter() - t, n_cells
+
+
+def run_reference(args):
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return
+    times = []
+    for i in range(args.warmup + args.steps):
+        dt, n = cpu_reference_sample(args.cpu_sample_cells, args, seed=100 + i)
+        if i >= args.warmup:
+            times.append(dt)
+    sec = float(np.mean(times))
+    value = args.cpu_sample_cells / sec
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "cells/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"{args.cells} cells x {args.features} features, ~{int(args.nnz)} nnz/cell binary CSR; "
+                               f"spectral n_comps={args.ncomps}", "sample_cells": args.cpu_sample_cells},
+        "cpu_baseline": {"value": value, "unit": "cells/s", "cores": 1, "kind": "port",
+                         "sample": f"{args.cpu_sample_cells}-cell sample of the same generator per step; "
+                                   "SciPy ARPACK eigsh with single-threaded sparse matvec, as the reference"},
+        "e2e": {"value": value, "unit": "cells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# --------------------------------------------------------------------------
+def run_gpu(args):
+    import torch
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+    import snapatac2_gb300 as snap
+    from snapatac2_gb300 import _eigen, synthetic as syn
+    from snapatac2_gb300._binning import DeviceCSR
+    from snapatac2_gb300.tools import spectral_embedding
+    from oracle import spectral as osp
+
+    counter = LaunchCounter()
+    n, m = args.cells, args.features
+    indptr, indices, _ = syn.binary_csr_device(n, m, nnz_per_cell=args.nnz, seed=1234 + rank, device=dev)
+    torch.cuda.synchronize(dev)
+    csr = DeviceCSR(indptr, indices, None, (n, m))
+    nnz = csr.nnz
+
+    def step(precision="mixed"):
+        return spectral_embedding(csr, None, args.ncomps, 0, precision=precision, block=args.block,
+                                  return_info=True)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize(dev)
+    # ---- timed region: device-resident input -------------------------------
+    _eigen.SPMM_EVENTS = []
+    counter.active = True
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier()
+    torch.cuda.synchronize(dev)
+    e_start, e_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e_start.record()
+    infos = []
+    for _ in range(args.steps):
+        ev, U, info = step()
+        infos.append(info)
+    e_end.record()
+    torch.cuda.synchronize(dev)
+    barrier()
+    clk = clocks.stop()
+    counter.active = False
+    ms = e_start.elapsed_time(e_end) / args.steps
+    spmm_ev = _eigen.SPMM_EVENTS
+    _eigen.SPMM_EVENTS = None
+    launches = counter.count
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = n * world / (ms / 1e3)
+
+    # SpMM roofline (dominant kernel), from the events of the timed region
+    t_time = x_time = 0.0
+    tb = xb = 0
+    for e0, e1, e2, op, code, b in spmm_ev:
+        t_time += e0.elapsed_time(e1)
+        x_time += e1.elapsed_time(e2)
+        a, c = _eigen.spmm_bytes(op, code, b)
+        tb += a
+        xb += c
+    n_launch = 2 * len(spmm_ev)
+    spmm_ms = (t_time + x_time) / max(n_launch, 1)
+    achieved = (tb + xb) / max((t_time + x_time) / 1e3, 1e-12) / 1e9
+    peak, peak_kind = peaks()
+    spmm_share = (t_time + x_time) / (ms * args.steps)
+
+    # ---- FP64 GPU form and accuracy of the mixed result --------------------
+    t0 = time.perf_counter()
+    for _ in range(args.fp64_steps):
+        ev64, U64, info64 = step("fp64")
+    torch.cuda.synchronize(dev)
+    ms64 = (time.perf_counter() - t0) * 1e3 / max(args.fp64_steps, 1)
+    pos, pos64 = ev > 0, ev64 > 0
+    kk = int(min(pos.sum(), pos64.sum()))
+    o, o64 = np.argsort(-ev)[:kk], np.argsort(-ev64)[:kk]
+    evrel = float(np.max(np.abs(ev[o] - ev64[o64]) / np.abs(ev64[o64]))) if kk else None
+    Ua, Ub = U.cpu().numpy()[:, o], U64.cpu().numpy()[:, o64]
+    ang = osp.eigvec_angles(ev[o], Ua, ev64[o64], Ub, rel_gap=1e-3) if kk else np.array([np.nan])
+    res64 = max(info64["residuals"]) if info64.get("residuals") else None
+
+    # ---- end to end through the public API (pinned host CSR) ---------------
+    host = DeviceCSR(indptr.cpu().pin_memory(), indices.cpu().pin_memory(), None, (n, m))
+    ad = snap.AnnData(n_obs=n, n_vars=m)
+    ad.X = host
+    h2d = host.indptr.numel() * 8 + host.indices.numel() * 4
+    snap.tl.spectral(ad, features=None, n_comps=args.ncomps, block=args.block)  # warm
+    barrier()
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        snap.tl.spectral(ad, features=None, n_comps=args.ncomps, block=args.block)
+    torch.cuda.synchronize(dev)
+    e2e_ms = (time.perf_counter() - t0) * 1e3 / args.e2e_steps
+    d2h = int(ad.obsm["X_spectral"].size * 8 + ad.uns["spectral_eigenvalue"].size * 8)
+    if world > 1:
+        t = torch.tensor([e2e_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+
+    if rank != 0:
+        if world > 1:
+            torch.distributed.destroy_process_group()
+        return
+    cpu = None
+    if not args.no_cpu_baseline and world == 1:
+        dt, ns = cpu_reference_sample(args.cpu_sample_cells, args, seed=100)
+        cpu = {"value": ns / dt, "unit": "cells/s", "cores": 1, "kind": "port",
+               "sample": f"{ns} cells of the same generator ({args.features} features, ~{int(args.nnz)} nnz/cell): "
+                         "IDF/normalise/degree + SciPy ARPACK eigsh (single-threaded sparse matvec, as the reference)"}
+    info = infos[-1]
+    line = {
+        "metric": METRIC, "value": value, "unit": "cells/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"spectral embedding, {n} cells x {m} features, ~{int(args.nnz)} nnz/cell binary CSR "
+                               f"(nnz={nnz}), n_comps={args.ncomps}, mixed precision",
+                   "parallelism": "replicas" if world > 1 else "single GPU", "block": args.block,
+                   "l2": "inputs larger than L2 (CSR indices 4 B x nnz)",
+                   "block_matvecs": info["block_matvecs"], "restarts": info["restarts"], "basis": info["basis"]},
+        "e2e": {"value": n * world / (e2e_ms / 1e3), "unit": "cells/s", "ms_per_step": e2e_ms,
+                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": d2h},
+        "fp64_gpu": {"value": n / (ms64 / 1e3), "unit": "cells/s", "ms_per_step": ms64,
+                     "block_matvecs": info64["block_matvecs"], "max_residual": res64},
+        "mixed_over_fp64": ms64 / ms,
+        "accuracy_vs_fp64_gpu": {"n_positive": kk, "eval_rel_err_max": evrel,
+                                 "principal_angle_max_rad": float(np.nanmax(ang))},
+        "roofline": {"kernel": "spmm_kernel (Gram matvec, Xᵀ gather over CSC + X gather over CSR)",
+                     "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_source": peak_kind,
+                     "traffic": None, "launches": n_launch, "avg_launch_ms": spmm_ms,
+                     "bytes_per_block_matvec": int((tb + xb) / max(len(spmm_ev), 1)),
+                     "share_of_step": spmm_share},
+        "gpu_launches": launches,
+        "clocks": clk,
+    }
+    if cpu is not None:
+        line["cpu_baseline"] = cpu
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

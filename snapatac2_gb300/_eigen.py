@@ -66,11 +66,43 @@ class GramOperator:
         w2, a, dinv = self.scales(dtype_code)
         cv = self.cvalues.data_ptr() if self.cvalues is not None else None
         v = self.csr.data.data_ptr() if self.csr.data is not None else None
+        ev = SPMM_EVENTS
+        if ev is not None:
+            e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+            e0.record()
         _lib.check(L.sg_spmm(dtype_code, block, self.m, self.colptr.data_ptr(), self.rowidx.data_ptr(), cv,
                              Zs.data_ptr(), T.data_ptr(), w2.data_ptr(), None, None, -1, stream), "sg_spmm (Xᵀ)")
+        if ev is not None:
+            e1.record()
         _lib.check(L.sg_spmm(dtype_code, block, self.n, self.csr.indptr.data_ptr(), self.csr.indices.data_ptr(), v,
                              T.data_ptr(), W.data_ptr(), a.data_ptr(), dinv.data_ptr(), Z.data_ptr(), -1, stream),
                    "sg_spmm (X)")
+        if ev is not None:
+            e2.record()
+            ev.append((e0, e1, e2, self, dtype_code, block))
+
+
+# When a list, GramOperator.apply records (start, mid, end) CUDA events around
+# its two SpMM launches, for live per-launch timing by the benchmark.
+SPMM_EVENTS: list | None = None
+
+
+def spmm_bytes(op: "GramOperator", dtype_code: int, block: int) -> tuple[int, int]:
+    """Algorithmic bytes of the two SpMM launches of one block matvec.
+
+    Xᵀ pass (rows = m, CSC): column pointers 8(m+1), row indices 4 nnz,
+    values 4 nnz if present, gathered input Zs read once 4b·n, output T
+    written 4b·m, scale 4m.  X pass (rows = n, CSR): 8(n+1) + 4 nnz (+4 nnz),
+    T read once 4b·m, W written 4b·n, Z read 4b·n, scale + shift 8n.
+    (Element size 8 instead of 4 for the FP64 form.)
+    """
+    e = 4 if dtype_code == 0 else 8
+    nnz = op.csr.nnz
+    vb = 4 * nnz if op.csr.data is not None else 0
+    n, m, b = op.n, op.m, block
+    t_pass = 8 * (m + 1) + 4 * nnz + vb + e * b * n + e * b * m + e * m
+    x_pass = 8 * (n + 1) + 4 * nnz + vb + e * b * m + 2 * e * b * n + 2 * e * n
+    return t_pass, x_pass
 
 
 def select_columns(csr: DeviceCSR, features: np.ndarray | None) -> DeviceCSR:

@@ -58,6 +58,16 @@ SIGNATURES: dict[str, tuple] = {
     "sg_basis_rotate": (_I32, [_I32, _I32, _I64, _P, _I64, _I32, _P, _I64, _I32, _P, _I64, _P]),
 }
 
+# Kernels launched by one call of each entry point (launch accounting of the
+# benchmark): e.g. sg_block_cholqr = projection partial + reduce + Cholesky +
+# R⁻¹ application.
+KERNELS_PER_CALL = {
+    "sg_tile_plan": 4, "sg_tile_run": 5, "sg_tile_emit": 1, "sg_csr_select_cols": 5,
+    "sg_csr_transpose": 7, "sg_spectral_prepare": 7, "sg_spmm": 1, "sg_block_proj": 2,
+    "sg_block_update": 1, "sg_block_cholqr": 4, "sg_block_finish": 1, "sg_lanczos_hblock": 1,
+    "sg_basis_rotate": 1, "sg_fill_random": 1, "sg_knn": 6,
+}
+
 _lock = threading.Lock()
 _lib: ctypes.CDLL | None = None
 

@@ -157,6 +157,24 @@ class BinaryCSR:
         return int(self.indices.shape[0])
 
 
+def _oversample_factor(n_features, nnz_per_cell, n_enr, cdf, p_enriched, rng) -> float:
+    """Draws per wanted unique feature, from a 200-row pilot (collisions of
+    the Zipf-weighted enriched draws make unique < draws)."""
+    factor = 1.0
+    enr = rng.choice(n_features, n_enr, replace=False)
+    for _ in range(3):
+        d = int(round(nnz_per_cell * factor))
+        uniq = []
+        for _r in range(200):
+            is_e = rng.random(d) < p_enriched
+            col = rng.integers(0, n_features, d)
+            ne = int(is_e.sum())
+            col[is_e] = enr[np.searchsorted(cdf, rng.random(ne), side="right").clip(0, n_enr - 1)]
+            uniq.append(np.unique(col).size)
+        factor *= nnz_per_cell / max(float(np.mean(uniq)), 1.0)
+    return factor
+
+
 def binary_csr(
     n_cells: int,
     n_features: int = 500_000,
@@ -170,19 +188,23 @@ def binary_csr(
     seed: int = 0,
     chunk_cells: int = 20_000,
 ) -> BinaryCSR:
-    """Binary CSR with ~``nnz_per_cell`` distinct features per row.
+    """Binary CSR with ~``nnz_per_cell`` distinct features per row (mean).
 
-    Per row, ``d`` ~ LogNormal(ln(nnz_per_cell), sigma) features are drawn
-    (``p_enriched`` of them Zipf-ranked from the cluster's enriched set, the
-    rest uniform) and de-duplicated.
+    Per row, the target ``t`` ~ LogNormal(ln(nnz_per_cell), sigma); ``t * f``
+    features are drawn (``p_enriched`` of them Zipf-ranked from the cluster's
+    enriched set, the rest uniform) and de-duplicated, with the oversampling
+    factor ``f`` set from a pilot so that rows average ``nnz_per_cell``
+    distinct features.
     """
     rng = np.random.Generator(np.random.PCG64(seed))
     n_enr = min(enriched, n_features)
-    draws = np.maximum(1, np.rint(rng.lognormal(np.log(nnz_per_cell), sigma, n_cells))).astype(np.int64)
-    draws = np.minimum(draws, n_features)
+    cdf = _zipf_cdf(n_enr, zipf_a)
+    factor = _oversample_factor(n_features, nnz_per_cell, n_enr, cdf, p_enriched,
+                                np.random.Generator(np.random.PCG64(seed + 1)))
+    draws = np.maximum(1, np.rint(factor * rng.lognormal(np.log(nnz_per_cell), sigma, n_cells))).astype(np.int64)
+    draws = np.minimum(draws, 4 * n_features)
     clusters = rng.integers(0, n_clusters, n_cells).astype(np.int32)
     enr = np.stack([rng.choice(n_features, n_enr, replace=False) for _ in range(n_clusters)]).astype(np.int64)
-    cdf = _zipf_cdf(n_enr, zipf_a)
     rows_idx = []
     row_nnz = np.zeros(n_cells, dtype=np.int64)
     for c0 in range(0, n_cells, chunk_cells):
@@ -202,3 +224,60 @@ def binary_csr(
     indptr = np.zeros(n_cells + 1, dtype=np.int64)
     np.cumsum(row_nnz, out=indptr[1:])
     return BinaryCSR(indptr=indptr, indices=np.concatenate(rows_idx), n_cols=n_features, clusters=clusters)
+
+
+def binary_csr_device(
+    n_cells: int,
+    n_features: int = 500_000,
+    *,
+    nnz_per_cell: float = 4_000.0,
+    sigma: float = 0.3,
+    n_clusters: int = 8,
+    enriched: int = 50_000,
+    zipf_a: float = 1.1,
+    p_enriched: float = 0.7,
+    seed: int = 0,
+    device=None,
+    chunk_cells: int = 25_000,
+):
+    """Same model as ``binary_csr``, drawn on the GPU with torch (fast input
+    generation for the large workloads; a different random stream than the
+    NumPy generator).  Returns (indptr int64, indices int32) CUDA tensors.
+    """
+    import torch
+    dev = torch.device(device) if device is not None else torch.device("cuda")
+    rng = np.random.Generator(np.random.PCG64(seed))
+    n_enr = min(enriched, n_features)
+    cdf_np = _zipf_cdf(n_enr, zipf_a)
+    factor = _oversample_factor(n_features, nnz_per_cell, n_enr, cdf_np, p_enriched,
+                                np.random.Generator(np.random.PCG64(seed + 1)))
+    draws = np.maximum(1, np.rint(factor * rng.lognormal(np.log(nnz_per_cell), sigma, n_cells))).astype(np.int64)
+    draws = np.minimum(draws, 4 * n_features)
+    clusters = rng.integers(0, n_clusters, n_cells).astype(np.int64)
+    enr = np.stack([rng.choice(n_features, n_enr, replace=False) for _ in range(n_clusters)]).astype(np.int64)
+    g = torch.Generator(device=dev)
+    g.manual_seed(int(seed))
+    cdf = torch.from_numpy(cdf_np).to(dev)
+    enr_t = torch.from_numpy(enr).to(dev)
+    cl_t = torch.from_numpy(clusters).to(dev)
+    row_nnz = torch.zeros(n_cells, dtype=torch.int64, device=dev)
+    parts = []
+    for c0 in range(0, n_cells, chunk_cells):
+        c1 = min(n_cells, c0 + chunk_cells)
+        d = torch.from_numpy(draws[c0:c1]).to(dev)
+        D = int(draws[c0:c1].sum())
+        cell = torch.repeat_interleave(torch.arange(c0, c1, device=dev), d)
+        is_enr = torch.rand(D, generator=g, device=dev) < p_enriched
+        col = torch.randint(0, n_features, (D,), generator=g, device=dev)
+        u = torch.rand(D, generator=g, device=dev, dtype=torch.float64)
+        rank = torch.searchsorted(cdf, u, right=True).clamp_(0, n_enr - 1)
+        ecol = enr_t[cl_t[cell], rank]
+        col = torch.where(is_enr, ecol, col)
+        key = torch.unique(cell * n_features + col)  # sorted, de-duplicated
+        r = key // n_features
+        parts.append((key - r * n_features).to(torch.int32))
+        row_nnz[c0:c1] = torch.bincount(r - c0, minlength=c1 - c0)
+        del cell, is_enr, col, u, rank, ecol, key, r
+    indptr = torch.zeros(n_cells + 1, dtype=torch.int64, device=dev)
+    torch.cumsum(row_nnz, 0, out=indptr[1:])
+    return indptr, torch.cat(parts), clusters

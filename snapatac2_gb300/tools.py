@@ -27,7 +27,17 @@ def _device(device=None) -> torch.device:
 
 
 def csr_to_device(X, device) -> DeviceCSR:
-    """Upload a scipy CSR matrix (values kept only when not all equal to 1)."""
+    """The matrix as a DeviceCSR on ``device``.
+
+    Accepts a scipy CSR matrix (values kept only when not all equal to 1) or
+    a DeviceCSR whose tensors live on the host (pinned memory gives
+    asynchronous copies) or already on the device.
+    """
+    if isinstance(X, DeviceCSR):
+        if X.indptr.device == device:
+            return X
+        mv = lambda t: None if t is None else t.to(device, non_blocking=True)  # noqa: E731
+        return DeviceCSR(mv(X.indptr), mv(X.indices), mv(X.data), X.shape)
     X = sp.csr_matrix(X)
     if not X.has_sorted_indices:
         X = X.copy()
@@ -54,7 +64,7 @@ def spectral_embedding(X, features=None, n_comps: int = 30, random_state: int = 
     ``X`` is a scipy CSR matrix or a ``DeviceCSR`` already on the GPU.
     """
     dev = _device(device)
-    csr = X if isinstance(X, DeviceCSR) else csr_to_device(X, dev)
+    csr = csr_to_device(X, dev)
     csr = _eigen.select_columns(csr, features)
     op = _eigen.build_operator(csr, feature_weights)
     res = _eigen.eigsh_lm(op, n_comps, precision=precision, block=block, seed=random_state, **solver_kw)
