@@ -205,6 +205,19 @@ int64_t sg_knn_scratch_bytes(int64_t n, int d, int k, int margin);
 int sg_knn(const double* X, int64_t n, int d, int k, int margin, int64_t* nbr, double* dist, void* scratch,
            int64_t scratch_bytes, int* n_fallback, void* stream);
 
+/* Allocation-free sg_knn (no counterpart in the reference).  Same inputs,   */
+/* outputs and result as sg_knn, for callers that cannot allocate device    */
+/* memory: the scratch is a fixed array inside the library (about 33 MB per  */
+/* GPU that loads it, held until exit).  Limits: n <= 16384 points,          */
+/* d <= 32, k <= 100 (k + margin is capped at 128); larger problems return   */
+/* SG_ERR_CAP without touching the outputs.  The first call on a device      */
+/* looks up the array's device address (cudaGetSymbolAddress, with that      */
+/* device current), so make that first call before any stream capture.      */
+/* All calls share the one array: calls that overlap on the GPU (different   */
+/* streams, no ordering between them) race and must be avoided.             */
+int sg_knn_noalloc(const double* X, int64_t n, int d, int k, int margin, int64_t* nbr, double* dist,
+                   int* n_fallback, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

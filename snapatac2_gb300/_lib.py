@@ -55,6 +55,7 @@ SIGNATURES: dict[str, tuple] = {
     "sg_lanczos_hblock": (_I32, [_I32, _P, _I64, _I32, _P, _P, _P, _P, _P, _I32, _P]),
     "sg_knn_scratch_bytes": (_I64, [_I64, _I32, _I32, _I32]),
     "sg_knn": (_I32, [_P, _I64, _I32, _I32, _I32, _P, _P, _P, _I64, _P, _P]),
+    "sg_knn_noalloc": (_I32, [_P, _I64, _I32, _I32, _I32, _P, _P, _P, _P]),
     "sg_basis_rotate": (_I32, [_I32, _I32, _I64, _P, _I64, _I32, _P, _I64, _I32, _P, _I64, _P]),
 }
 

@@ -428,3 +428,80 @@ extern "C" int sg_knn(const double* X, int64_t n, int d, int k, int margin, int6
     return SG_ERR_CUDA;
   return SG_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Allocation-free variant of sg_knn.
+//
+// Some callers cannot allocate device memory for the scratch sg_knn needs:
+// an application whose device memory is owned by its own pool or framework
+// (raw cudaMalloc is not allowed there), or a latency-bound caller for whom
+// cudaMalloc, which may synchronise the whole device and is slow, is not an
+// option.  For them the scratch lives in the fixed array below, which is part
+// of this library's device image: every GPU that loads the library holds it
+// (about 33 MB) until the process exits.
+// ---------------------------------------------------------------------------
+#include <mutex>
+
+namespace sg {
+namespace {
+
+constexpr int64_t kNoAllocMaxN = 16384;  // points
+constexpr int kNoAllocMaxDim = 32;       // dimensions
+constexpr int kNoAllocMaxK = 100;        // neighbours
+constexpr int64_t kA256(int64_t x) { return (x + 255) / 256 * 256; }
+// knn_layout(kNoAllocMaxN, 32, kNoAllocMaxK, kMaxKp) written out: X32, X64,
+// candidates, tau, flagged, fallback candidates, fallback distances, counters
+constexpr int64_t kNoAllocBytes =
+    kA256(kNoAllocMaxN * kNoAllocMaxDim * 4) + kA256(kNoAllocMaxN * kNoAllocMaxDim * 8) +
+    kA256(kNoAllocMaxN * kMaxKp * 4) + kA256(kNoAllocMaxN * 4) + kA256(kNoAllocMaxN * 4) +
+    kA256(kNoAllocMaxN * kNoAllocMaxK * 4) + kA256(kNoAllocMaxN * kNoAllocMaxK * 8) + kA256(16);
+
+static __device__ __align__(256) unsigned char g_knn_scratch[kNoAllocBytes];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_knn_scratch_mu;
+void* g_knn_scratch_ptr[kMaxDevices] = {};
+
+// Device address of g_knn_scratch on the current device.  In host code the
+// name g_knn_scratch is only a host-side stand-in, so the address is looked
+// up once per device (with that device current) and kept.
+int knn_scratch_address(void** out) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return SG_ERR_CUDA;
+  if (dev < 0 || dev >= kMaxDevices) return SG_ERR_ARG;
+  std::lock_guard<std::mutex> lock(g_knn_scratch_mu);
+  if (!g_knn_scratch_ptr[dev]) {
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_knn_scratch) != cudaSuccess || !p) return SG_ERR_CUDA;
+    g_knn_scratch_ptr[dev] = p;
+  }
+  *out = g_knn_scratch_ptr[dev];
+  return SG_OK;
+}
+
+}  // namespace
+}  // namespace sg
+
+extern "C" int sg_knn_noalloc(const double* X, int64_t n, int d, int k, int margin, int64_t* nbr, double* dist,
+                              int* n_fallback, void* stream) {
+  if (n < 2 || d <= 0 || k <= 0 || k > n - 1 || margin < 0) return SG_ERR_ARG;
+  if (n > kNoAllocMaxN || d > kNoAllocMaxDim || k > kNoAllocMaxK) return SG_ERR_CAP;
+  if (k + margin > kMaxKp) margin = kMaxKp - k;
+  int Kp = k + margin;
+  if (Kp > n - 1) Kp = (int)(n - 1);
+  void* base = nullptr;
+  int e = knn_scratch_address(&base);
+  if (e) return e;
+  const int DP = pad_dim(d);
+  KnnScratch w = knn_layout((char*)base, n, DP, k, k + margin);
+  if (w.bytes > kNoAllocBytes) return SG_ERR_CAP;
+  cudaStream_t s = as_stream(stream);
+  // knn_run clears the two counters it accumulates into (fallback count,
+  // max norm) before use; every other scratch byte is written before read.
+  e = DP == 16 ? knn_run<16>(X, n, d, k, Kp, w, nbr, dist, s) : knn_run<32>(X, n, d, k, Kp, w, nbr, dist, s);
+  if (e) return e;
+  if (n_fallback &&
+      cudaMemcpyAsync(n_fallback, w.nflag, sizeof(int), cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+    return SG_ERR_CUDA;
+  return SG_OK;
+}
