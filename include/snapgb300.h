@@ -120,15 +120,19 @@ int sg_csr_select_cols(int64_t n, const int64_t* indptr, const int32_t* indices,
                        const int32_t* colmap, int64_t* out_indptr, int32_t* out_indices, float* out_values,
                        void* scan_scratch, void* stream);
 
-/* Number of row blocks used by sg_csr_transpose (work = nblk * m int32).   */
+/* Number of row blocks used by sg_csr_transpose.                          */
 int sg_transpose_blocks(void);
+
+/* Bytes of scratch (256-B aligned) sg_csr_transpose needs.                 */
+int64_t sg_transpose_work_bytes(int64_t n, int64_t m, int nblk);
 
 /* Deterministic CSR -> CSC transpose (rows ascending in every column).     */
 /* colptr[m+1] (int64), rowidx[nnz], cvalues[nnz] (NULL if values NULL).     */
-/* Unsorted / duplicate / out-of-range column indices -> status SG_ERR_ARG.  */
+/* Unsorted / duplicate / out-of-range column indices -> status SG_ERR_ARG   */
+/* (the outputs are then not written).                                       */
 int sg_csr_transpose(int64_t n, int64_t m, const int64_t* indptr, const int32_t* indices,
-                     const float* values, int nblk, int32_t* work, int64_t* colptr, int32_t* rowidx,
-                     float* cvalues, void* scan_scratch, int* status, void* stream);
+                     const float* values, int nblk, void* work, int64_t work_bytes, int64_t* colptr,
+                     int32_t* rowidx, float* cvalues, void* scan_scratch, int* status, void* stream);
 
 /* Operator set-up in FP64: w = idf (or a copy of feature_weights when not  */
 /* NULL), w2 = w², rinv = 1/||(XW)_i||, colsum = 1ᵀXn, dinv = 1/(d - 1),    */
@@ -151,6 +155,13 @@ int sg_spectral_prepare(int64_t n, int64_t m, const int64_t* indptr, const int32
 int sg_spmm(int dtype, int block, int64_t rows, const int64_t* ptr, const int32_t* idx, const float* val,
             const void* in, void* out, const void* scale, const void* dshift, const void* y, int grid,
             void* stream);
+
+/* sg_spmm with an explicit memory-access variant in [0, sg_spmm_variants()) */
+/* (same arithmetic and result; an autotuner picks the fastest per shape).   */
+int sg_spmm_variants(void);
+int sg_spmm_ex(int dtype, int block, int64_t rows, const int64_t* ptr, const int32_t* idx, const float* val,
+               const void* in, void* out, const void* scale, const void* dshift, const void* y, int grid,
+               int variant, void* stream);
 
 /* ---- block Krylov-Schur (thick-restart block Lanczos) building blocks --- */
 /* Q: n x ldq row-major basis; W: n x block working block.                   */
@@ -204,6 +215,29 @@ int64_t sg_knn_scratch_bytes(int64_t n, int d, int k, int margin);
 
 int sg_knn(const double* X, int64_t n, int d, int k, int margin, int64_t* nbr, double* dist, void* scratch,
            int64_t scratch_bytes, int* n_fallback, void* stream);
+
+/* ------------------------------------------------------------------------ */
+/* Adjoint: gradient of the sum of the wanted eigenvalues of the cosine     */
+/* operator with respect to the feature weights (no counterpart in the      */
+/* reference, whose weights are fixed inputs, embedding.rs:42-47).  FP64.   */
+/* U: n x k eigenvectors (row-major), evals: k, dinv/rinv from              */
+/* sg_spectral_prepare.  Between the stages the caller runs sg_spmm in FP64:*/
+/*   stage1 -> [r s U | r δ̄ | r] (n x block)   ; CSC SpMM -> ZEH (m x block) */
+/*   stage2 -> [w² Z | w² e]     (m x block2)  ; CSR SpMM -> P   (n x block2)*/
+/*   stage3 -> [ρ̄ r, 0, 0, 0]    (n x 4)       ; CSC SpMM with squared      */
+/*                                              values -> g (m x 4)          */
+/*   final  -> grad[m]                                                       */
+/* ------------------------------------------------------------------------ */
+int sg_adjoint_stage1(int64_t n, int k, const double* U, const double* evals, const double* dinv,
+                      const double* rinv, int block, double* out, double* dbar, void* stream);
+int sg_adjoint_stage2(int64_t m, int k, const double* zeh, int block, const double* w, int block2, double* out,
+                      void* stream);
+int sg_adjoint_stage3(int64_t n, int k, const double* U, const double* dinv, const double* rinv,
+                      const double* dbar, const double* P, int block2, double* out, void* stream);
+int sg_adjoint_final(int64_t m, int k, const double* w, const double* zeh, int block, const double* g,
+                     double* grad, void* stream);
+/* out[t] = values[t]^2 (the X∘X values of the third SpMM). */
+int sg_square_values(int64_t nnz, const float* values, float* out, void* stream);
 
 /* Allocation-free sg_knn (no counterpart in the reference).  Same inputs,   */
 /* outputs and result as sg_knn, for callers that cannot allocate device    */

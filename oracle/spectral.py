@@ -98,33 +98,47 @@ def spectral(X: sp.csr_matrix, n_vars: int | None = None, features=None, n_comps
 
 
 def principal_angles(U: np.ndarray, V: np.ndarray) -> np.ndarray:
-    """Principal angles (radians) between the column spaces of U and V."""
+    """Principal angles (radians, descending) between the column spaces of U and V."""
     qu, _ = np.linalg.qr(U)
     qv, _ = np.linalg.qr(V)
-    s = np.linalg.svd(qu.T @ qv, compute_uv=False)
-    s = np.clip(s, -1.0, 1.0)
-    # arcsin of the sine form is accurate for small angles
-    proj = qv - qu @ (qu.T @ qv)
-    sn = np.linalg.svd(proj, compute_uv=False)
-    return np.sort(np.arcsin(np.clip(sn, 0.0, 1.0)))[::-1] if sn.size else np.arccos(s)
+    # sines of the angles = singular values of the part of V outside span(U):
+    # accurate for small angles, unlike arccos of the cosines
+    sn = np.linalg.svd(qv - qu @ (qu.T @ qv), compute_uv=False)
+    return np.sort(np.arcsin(np.clip(sn, 0.0, 1.0)))[::-1]
 
 
-def eigvec_angles(evals: np.ndarray, U: np.ndarray, evals_ref: np.ndarray, V: np.ndarray,
-                  rel_gap: float = 1e-3):
-    """Per-cluster principal angles between matching eigenvectors.
-
-    Eigenvalues of the reference closer than ``rel_gap`` (relative) are grouped
-    into clusters; each cluster's subspace is compared as a whole, which makes
-    the comparison independent of sign and of rotations inside a degenerate
-    cluster.  Returns the largest angle of each cluster.
-    """
-    k = min(U.shape[1], V.shape[1])
-    out = []
-    i = 0
+def eig_clusters(evals_ref: np.ndarray, rel_gap: float = 1e-3):
+    """Index ranges [i, j) of eigenvalues closer than rel_gap (relative)."""
+    k = len(evals_ref)
+    out, i = [], 0
     while i < k:
         j = i + 1
         while j < k and abs(evals_ref[j] - evals_ref[j - 1]) <= rel_gap * max(abs(evals_ref[j - 1]), 1e-300):
             j += 1
-        out.append(float(principal_angles(U[:, i:j], V[:, i:j]).max()))
+        out.append((i, j))
         i = j
-    return np.array(out)
+    return out
+
+
+def eigvec_angles(evals: np.ndarray, U: np.ndarray, evals_ref: np.ndarray, V: np.ndarray,
+                  rel_gap: float = 1e-3, next_eval: float | None = None, return_open: bool = False):
+    """Largest principal angle of each cluster of eigenvectors.
+
+    Eigenvalues of the reference closer than ``rel_gap`` (relative) form a
+    cluster whose subspace is compared as a whole (independent of sign and of
+    rotations inside a degenerate cluster).  If ``next_eval`` (the first
+    eigenvalue outside the compared set) is within ``rel_gap`` of the last
+    one, the last cluster is cut by the set boundary and its subspace is
+    ill-conditioned; with ``return_open`` its angle is returned separately as
+    (closed_angles, open_angle) instead of being mixed into the list.
+    """
+    k = min(U.shape[1], V.shape[1])
+    cl = eig_clusters(np.asarray(evals_ref)[:k], rel_gap)
+    ang = np.array([float(principal_angles(U[:, i:j], V[:, i:j]).max()) for i, j in cl])
+    if not return_open:
+        return ang
+    last = evals_ref[k - 1]
+    is_open = next_eval is not None and abs(next_eval - last) <= rel_gap * abs(last)
+    if is_open and len(ang) > 0:
+        return ang[:-1], float(ang[-1])
+    return ang, None

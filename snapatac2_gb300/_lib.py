@@ -42,10 +42,13 @@ SIGNATURES: dict[str, tuple] = {
     "sg_tile_emit": (_I32, [_I64, _P, _P, _I64, _P, _P, _P, _I64, _P, _P]),
     "sg_csr_select_cols": (_I32, [_I64, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
     "sg_transpose_blocks": (_I32, []),
-    "sg_csr_transpose": (_I32, [_I64, _I64, _P, _P, _P, _I32, _P, _P, _P, _P, _P, _P, _P]),
+    "sg_transpose_work_bytes": (_I64, [_I64, _I64, _I32]),
+    "sg_csr_transpose": (_I32, [_I64, _I64, _P, _P, _P, _I32, _P, _I64, _P, _P, _P, _P, _P, _P]),
     "sg_spectral_prepare": (_I32, [_I64, _I64, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P,
                                    _P, _P, _P, _P, _P, _P]),
     "sg_spmm": (_I32, [_I32, _I32, _I64, _P, _P, _P, _P, _P, _P, _P, _P, _I32, _P]),
+    "sg_spmm_variants": (_I32, []),
+    "sg_spmm_ex": (_I32, [_I32, _I32, _I64, _P, _P, _P, _P, _P, _P, _P, _P, _I32, _I32, _P]),
     "sg_proj_parts": (_I32, []),
     "sg_fill_random": (_I32, [_I32, _I64, ctypes.c_uint64, _P, _P]),
     "sg_block_proj": (_I32, [_I32, _I32, _I64, _P, _I64, _I32, _P, _P, _I32, _P, _P]),
@@ -56,6 +59,11 @@ SIGNATURES: dict[str, tuple] = {
     "sg_knn_scratch_bytes": (_I64, [_I64, _I32, _I32, _I32]),
     "sg_knn": (_I32, [_P, _I64, _I32, _I32, _I32, _P, _P, _P, _I64, _P, _P]),
     "sg_knn_noalloc": (_I32, [_P, _I64, _I32, _I32, _I32, _P, _P, _P, _P]),
+    "sg_adjoint_stage1": (_I32, [_I64, _I32, _P, _P, _P, _P, _I32, _P, _P, _P]),
+    "sg_adjoint_stage2": (_I32, [_I64, _I32, _P, _I32, _P, _I32, _P, _P]),
+    "sg_adjoint_stage3": (_I32, [_I64, _I32, _P, _P, _P, _P, _P, _I32, _P, _P]),
+    "sg_adjoint_final": (_I32, [_I64, _I32, _P, _P, _I32, _P, _P, _P]),
+    "sg_square_values": (_I32, [_I64, _P, _P, _P]),
     "sg_basis_rotate": (_I32, [_I32, _I32, _I64, _P, _I64, _I32, _P, _I64, _I32, _P, _I64, _P]),
 }
 
@@ -64,9 +72,15 @@ SIGNATURES: dict[str, tuple] = {
 # R⁻¹ application.
 KERNELS_PER_CALL = {
     "sg_tile_plan": 4, "sg_tile_run": 5, "sg_tile_emit": 1, "sg_csr_select_cols": 5,
-    "sg_csr_transpose": 7, "sg_spectral_prepare": 7, "sg_spmm": 1, "sg_block_proj": 2,
+    "sg_csr_transpose": 8, "sg_spectral_prepare": 7, "sg_spmm": 1, "sg_spmm_ex": 1, "sg_block_proj": 2,
     "sg_block_update": 1, "sg_block_cholqr": 4, "sg_block_finish": 1, "sg_lanczos_hblock": 1,
-    "sg_basis_rotate": 1, "sg_fill_random": 1, "sg_knn": 6,
+    "sg_adjoint_stage1": (_I32, [_I64, _I32, _P, _P, _P, _P, _I32, _P, _P, _P]),
+    "sg_adjoint_stage2": (_I32, [_I64, _I32, _P, _I32, _P, _I32, _P, _P]),
+    "sg_adjoint_stage3": (_I32, [_I64, _I32, _P, _P, _P, _P, _P, _I32, _P, _P]),
+    "sg_adjoint_final": (_I32, [_I64, _I32, _P, _P, _I32, _P, _P, _P]),
+    "sg_square_values": (_I32, [_I64, _P, _P, _P]),
+    "sg_basis_rotate": 1, "sg_fill_random": 1, "sg_knn": 6, "sg_adjoint_stage1": 1,
+    "sg_adjoint_stage2": 1, "sg_adjoint_stage3": 1, "sg_adjoint_final": 1, "sg_square_values": 1,
 }
 
 _lock = threading.Lock()

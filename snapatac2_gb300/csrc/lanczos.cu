@@ -268,14 +268,16 @@ __global__ void fill_random(int64_t count, uint64_t seed, T* __restrict__ out) {
 template <typename T, int B>
 int proj_t(int64_t n, const T* Q, int64_t ldq, int ncols, const T* W, double* part, int nparts, double* C,
            cudaStream_t s) {
-  if (ncols <= kProjBlock) proj_partial<T, B, 1><<<nparts, kProjBlock, 0, s>>>(n, Q, ldq, ncols, W, part);
-  else if (ncols <= 2 * kProjBlock) proj_partial<T, B, 2><<<nparts, kProjBlock, 0, s>>>(n, Q, ldq, ncols, W, part);
-  else if (ncols <= 4 * kProjBlock && B <= 8) proj_partial<T, B <= 8 ? B : 8, 4><<<nparts, kProjBlock, 0, s>>>(n, Q, ldq, ncols, W, part);
-  else return SG_ERR_ARG;
-  SG_CHECK_LAUNCH();
-  const int tot = ncols * B;
-  proj_reduce<<<(tot + 255) / 256, 256, 0, s>>>(nparts, ncols, B, part, C);
-  SG_CHECK_LAUNCH();
+  // column slices of at most 2 * kProjBlock basis vectors per launch
+  for (int c0 = 0; c0 < ncols; c0 += 2 * kProjBlock) {
+    const int nc = ncols - c0 < 2 * kProjBlock ? ncols - c0 : 2 * kProjBlock;
+    if (nc <= kProjBlock) proj_partial<T, B, 1><<<nparts, kProjBlock, 0, s>>>(n, Q + c0, ldq, nc, W, part);
+    else proj_partial<T, B, 2><<<nparts, kProjBlock, 0, s>>>(n, Q + c0, ldq, nc, W, part);
+    SG_CHECK_LAUNCH();
+    const int tot = nc * B;
+    proj_reduce<<<(tot + 255) / 256, 256, 0, s>>>(nparts, nc, B, part, C + (int64_t)c0 * B);
+    SG_CHECK_LAUNCH();
+  }
   return SG_OK;
 }
 

@@ -61,24 +61,76 @@ __global__ void select_fill(int64_t n, const int64_t* __restrict__ ptr, const in
 
 // ---------------------------------------------------------------------------
 // deterministic transpose (CSR -> CSC) with rows ascending inside each column
+//
+// Columns are cut into panels of kTrPanel columns so that a CTA keeps the
+// counters / cursors of one panel in shared memory.  seg[r][p] is the offset
+// (from the row start) of row r's first entry in panel p (rows are sorted, so
+// a row's entries of one panel are contiguous).  Rows are split into nblk row
+// blocks; for every (row block, panel):
+//   count : shared-memory histogram of the panel's columns, written to
+//           cnt[b][col] (coalesced);
+//   offsets: cnt[b][col] <- sum over earlier row blocks (column-wise scan);
+//   fill  : the CTA walks its rows in order and appends each row index to
+//           its column (one entry per column per row, so no two threads touch
+//           the same cursor inside a row; rows are separated by a barrier).
+// Row order inside every column is therefore ascending and the result is
+// identical run to run.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(512) tr_count(int64_t n, int64_t m, const int64_t* __restrict__ ptr,
-                                                const int32_t* __restrict__ idx, int nblk,
-                                                int32_t* __restrict__ cnt, int* status) {
-  const int b = blockIdx.x;
-  const int64_t r0 = n * b / nblk, r1 = n * (b + 1) / nblk;
-  int32_t* c = cnt + (int64_t)b * m;
-  for (int64_t r = r0; r < r1; ++r) {
+constexpr int kTrPanel = 16384;
+
+__global__ void seg_kernel(int64_t n, const int64_t* __restrict__ ptr, const int32_t* __restrict__ idx, int pw,
+                           int P, int64_t m, int32_t* __restrict__ seg, int* status) {
+  const int lane = threadIdx.x & 31;
+  const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t r = gw; r < n; r += nw) {
     const int64_t s = ptr[r], e = ptr[r + 1];
-    for (int64_t k = s + threadIdx.x; k < e; k += blockDim.x) {
-      const int j = idx[k];
-      if (j < 0 || j >= m || (k > s && idx[k - 1] >= j)) {  // need sorted, unique, in range
-        report_error(status, nullptr, SG_ERR_ARG, 0);
-        continue;
+    int32_t* sg = seg + r * (int64_t)(P + 1);
+    const int len = (int)(e - s);
+    for (int64_t k0 = s; k0 < e + 1; k0 += 32) {
+      const int64_t k = k0 + lane;
+      if (k > e) continue;
+      // panel of this entry (P for the end sentinel) and of the previous one
+      int pc = P, pp = -1;
+      if (k < e) {
+        const int c = idx[k];
+        if (c < 0 || c >= m || (k > s && idx[k - 1] >= c)) {  // need sorted, unique, in range
+          report_error(status, nullptr, SG_ERR_ARG, 0);
+          pc = P;
+        } else {
+          pc = c / pw;
+        }
       }
-      atomicAdd(c + j, 1);
+      if (k > s) {
+        const int cprev = idx[k - 1];
+        pp = (cprev >= 0 && cprev < m) ? cprev / pw : P;
+      }
+      for (int p = pp + 1; p <= pc && p <= P; ++p) sg[p] = (int32_t)(k - s);
     }
+    if (len == 0 && lane == 0)
+      for (int p = 0; p <= P; ++p) sg[p] = 0;
   }
+}
+
+__global__ void __launch_bounds__(512)
+tr_count(int64_t n, int64_t m, const int64_t* __restrict__ ptr, const int32_t* __restrict__ idx,
+         const int32_t* __restrict__ seg, int P, int nblk, int32_t* __restrict__ cnt, const int* status) {
+  __shared__ int32_t c_s[kTrPanel];
+  if (*status) return;  // invalid column indices: seg is not trustworthy
+  const int b = blockIdx.x, p = blockIdx.y;
+  const int64_t r0 = n * b / nblk, r1 = n * (b + 1) / nblk;
+  const int64_t col0 = (int64_t)p * kTrPanel;
+  const int width = (int)min((int64_t)kTrPanel, m - col0);
+  for (int j = threadIdx.x; j < width; j += blockDim.x) c_s[j] = 0;
+  __syncthreads();
+  for (int64_t r = r0; r < r1; ++r) {
+    const int32_t* sg = seg + r * (int64_t)(P + 1);
+    const int64_t s = ptr[r] + sg[p], e = ptr[r] + sg[p + 1];
+    for (int64_t k = s + threadIdx.x; k < e; k += blockDim.x) atomicAdd(&c_s[idx[k] - col0], 1);
+  }
+  __syncthreads();
+  int32_t* out = cnt + (int64_t)b * m + col0;
+  for (int j = threadIdx.x; j < width; j += blockDim.x) out[j] = c_s[j];
 }
 
 // colptr[j+1] = total count of column j
@@ -91,53 +143,43 @@ __global__ void tr_total(int64_t m, int nblk, const int32_t* __restrict__ cnt, i
   }
 }
 
-// cnt[b][j] <- colptr[j] + sum_{b' < b} cnt[b'][j]  (cursor of row block b)
-__global__ void tr_offsets(int64_t m, int nblk, int32_t* __restrict__ cnt, const int64_t* __restrict__ colptr,
-                           int64_t* __restrict__ cur) {
+// cnt[b][j] <- sum_{b' < b} cnt[b'][j]  (row block b's offset inside column j)
+__global__ void tr_offsets(int64_t m, int nblk, int32_t* __restrict__ cnt) {
   for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < m; j += (int64_t)gridDim.x * blockDim.x) {
     int64_t run = 0;
     for (int b = 0; b < nblk; ++b) {
       const int64_t c = cnt[(int64_t)b * m + j];
-      cnt[(int64_t)b * m + j] = (int32_t)run;  // offset inside the column
+      cnt[(int64_t)b * m + j] = (int32_t)run;
       run += c;
     }
-    (void)cur;
   }
 }
 
-constexpr int kFillBlock = 512;
-constexpr int kFillItems = 8;
-
-__global__ void __launch_bounds__(kFillBlock)
+__global__ void __launch_bounds__(512)
 tr_fill(int64_t n, int64_t m, const int64_t* __restrict__ ptr, const int32_t* __restrict__ idx,
-        const float* __restrict__ val, int nblk, int32_t* __restrict__ cnt, const int64_t* __restrict__ colptr,
-        int32_t* __restrict__ rowidx, float* __restrict__ cval, int* status) {
+        const float* __restrict__ val, const int32_t* __restrict__ seg, int P, int nblk,
+        const int32_t* __restrict__ cnt, const int64_t* __restrict__ colptr, int32_t* __restrict__ rowidx,
+        float* __restrict__ cval, const int* status) {
+  __shared__ int32_t cur[kTrPanel];
   if (*status) return;
-  const int b = blockIdx.x;
+  const int b = blockIdx.x, p = blockIdx.y;
   const int64_t r0 = n * b / nblk, r1 = n * (b + 1) / nblk;
-  int32_t* c = cnt + (int64_t)b * m;
+  const int64_t col0 = (int64_t)p * kTrPanel;
+  const int width = (int)min((int64_t)kTrPanel, m - col0);
+  const int32_t* in = cnt + (int64_t)b * m + col0;
+  for (int j = threadIdx.x; j < width; j += blockDim.x) cur[j] = in[j];
+  __syncthreads();
   for (int64_t r = r0; r < r1; ++r) {
-    const int64_t s = ptr[r], e = ptr[r + 1];
-    for (int64_t k0 = s; k0 < e; k0 += (int64_t)kFillBlock * kFillItems) {
-      int j[kFillItems];
-      int p[kFillItems];
-#pragma unroll
-      for (int t = 0; t < kFillItems; ++t) {
-        const int64_t k = k0 + (int64_t)t * kFillBlock + threadIdx.x;
-        j[t] = k < e ? idx[k] : -1;
-      }
-#pragma unroll
-      for (int t = 0; t < kFillItems; ++t) p[t] = j[t] >= 0 ? c[j[t]] : 0;
-#pragma unroll
-      for (int t = 0; t < kFillItems; ++t) {
-        if (j[t] >= 0) {
-          const int64_t k = k0 + (int64_t)t * kFillBlock + threadIdx.x;
-          c[j[t]] = p[t] + 1;
-          const int64_t dst = colptr[j[t]] + p[t];
-          rowidx[dst] = (int32_t)r;
-          if (cval) cval[dst] = val[k];
-        }
-      }
+    const int32_t* sg = seg + r * (int64_t)(P + 1);
+    const int64_t s = ptr[r] + sg[p], e = ptr[r] + sg[p + 1];
+    for (int64_t k = s + threadIdx.x; k < e; k += blockDim.x) {
+      const int c = idx[k];
+      const int j = c - (int)col0;
+      const int pos = cur[j];
+      cur[j] = pos + 1;
+      const int64_t dst = colptr[c] + pos;
+      rowidx[dst] = (int32_t)r;
+      if (cval) cval[dst] = val[k];
     }
     __syncthreads();  // the next row may touch the same columns
   }
@@ -296,7 +338,16 @@ template <> struct V16<double> {
   }
 };
 
-template <typename T, int B, bool VALUED, bool SHIFT>
+// Variants (same arithmetic, same result, picked by the autotuner): bits 0-1
+// select 1, 2, 4 or 8 chunks of 32 column indices in flight per iteration
+// (more gathers outstanding per lane against fewer resident warps); bit 2
+// sends the gathers through L2 only (ld.global.cg).
+template <typename VT>
+__device__ __forceinline__ VT gather16(const VT* p, bool l2only) {
+  return l2only ? __ldcg(p) : __ldg(p);
+}
+
+template <typename T, int B, bool VALUED, bool SHIFT, int VAR>
 __global__ void __launch_bounds__(256)
 spmm_kernel(int64_t rows, const int64_t* __restrict__ ptr, const int32_t* __restrict__ idx,
             const float* __restrict__ val, const T* __restrict__ in, T* __restrict__ out,
@@ -305,7 +356,9 @@ spmm_kernel(int64_t rows, const int64_t* __restrict__ ptr, const int32_t* __rest
   constexpr int VW = V16<T>::n;
   constexpr int LPN = B / VW;          // lanes per nonzero
   constexpr int NPS = 32 / LPN;        // nonzeros per warp step
-  constexpr int CH = LPN >= 4 ? 1 : 4 / LPN;  // 32-index chunks per iteration
+  constexpr int CH = 1 << (VAR & 3);   // 32-index chunks per iteration
+  constexpr bool L2ONLY = (VAR & 4) != 0;
+  constexpr bool STREAM = false;
   static_assert(B % VW == 0 && LPN >= 1 && LPN <= 32, "unsupported block width");
   const int lane = threadIdx.x & 31;
   const int sub = lane % LPN, slot = lane / LPN;
@@ -320,20 +373,18 @@ spmm_kernel(int64_t rows, const int64_t* __restrict__ ptr, const int32_t* __rest
 #pragma unroll
       for (int c = 0; c < CH; ++c) {
         const int64_t k = base + c * 32 + lane;
-        ci[c] = k < e ? __ldg(idx + k) : -1;
-        cv[c] = (VALUED && k < e) ? __ldg(val + k) : 1.0f;
+        ci[c] = k < e ? (STREAM ? __ldcs(idx + k) : __ldg(idx + k)) : -1;
+        cv[c] = (VALUED && k < e) ? (STREAM ? __ldcs(val + k) : __ldg(val + k)) : 1.0f;
       }
       VT g[CH * LPN];
-      int gc[CH * LPN];
       float gv[CH * LPN];
 #pragma unroll
       for (int c = 0; c < CH; ++c)
 #pragma unroll
         for (int j = 0; j < LPN; ++j) {
           const int col = __shfl_sync(0xffffffffu, ci[c], j * NPS + slot);
-          gc[c * LPN + j] = col;
           if (VALUED) gv[c * LPN + j] = __shfl_sync(0xffffffffu, cv[c], j * NPS + slot);
-          g[c * LPN + j] = col >= 0 ? __ldg(reinterpret_cast<const VT*>(in + (int64_t)col * B) + sub)
+          g[c * LPN + j] = col >= 0 ? gather16(reinterpret_cast<const VT*>(in + (int64_t)col * B) + sub, L2ONLY)
                                     : V16<T>::zero();
         }
 #pragma unroll
@@ -348,46 +399,61 @@ spmm_kernel(int64_t rows, const int64_t* __restrict__ ptr, const int32_t* __rest
       const T sc = scale[r];
       T* op = out + r * B + sub * VW;
       const T* a = reinterpret_cast<const T*>(&acc);
+      VT o;
+      T* ov = reinterpret_cast<T*>(&o);
       if (SHIFT) {
         const T d = dshift[r];
         const T* yp = y + r * B + sub * VW;
-        VT o;
-        T* ov = reinterpret_cast<T*>(&o);
 #pragma unroll
         for (int q = 0; q < VW; ++q) ov[q] = sc * a[q] - d * yp[q];
-        *reinterpret_cast<VT*>(op) = o;
       } else {
-        VT o;
-        T* ov = reinterpret_cast<T*>(&o);
 #pragma unroll
         for (int q = 0; q < VW; ++q) ov[q] = sc * a[q];
-        *reinterpret_cast<VT*>(op) = o;
       }
+      *reinterpret_cast<VT*>(op) = o;
     }
   }
 }
 
-template <typename T, int B>
-int launch_spmm_t(int64_t rows, const int64_t* ptr, const int32_t* idx, const float* val, const T* in,
-                  T* out, const T* scale, const T* dshift, const T* y, int grid, cudaStream_t s) {
+constexpr int kSpmmVariants = 8;
+
+template <typename T, int B, int VAR>
+void launch_spmm_v(int64_t rows, const int64_t* ptr, const int32_t* idx, const float* val, const T* in, T* out,
+                   const T* scale, const T* dshift, const T* y, int grid, cudaStream_t s) {
   if (val) {
-    if (dshift) spmm_kernel<T, B, true, true><<<grid, 256, 0, s>>>(rows, ptr, idx, val, in, out, scale, dshift, y);
-    else spmm_kernel<T, B, true, false><<<grid, 256, 0, s>>>(rows, ptr, idx, val, in, out, scale, dshift, y);
+    if (dshift) spmm_kernel<T, B, true, true, VAR><<<grid, 256, 0, s>>>(rows, ptr, idx, val, in, out, scale, dshift, y);
+    else spmm_kernel<T, B, true, false, VAR><<<grid, 256, 0, s>>>(rows, ptr, idx, val, in, out, scale, dshift, y);
   } else {
-    if (dshift) spmm_kernel<T, B, false, true><<<grid, 256, 0, s>>>(rows, ptr, idx, val, in, out, scale, dshift, y);
-    else spmm_kernel<T, B, false, false><<<grid, 256, 0, s>>>(rows, ptr, idx, val, in, out, scale, dshift, y);
+    if (dshift) spmm_kernel<T, B, false, true, VAR><<<grid, 256, 0, s>>>(rows, ptr, idx, val, in, out, scale, dshift, y);
+    else spmm_kernel<T, B, false, false, VAR><<<grid, 256, 0, s>>>(rows, ptr, idx, val, in, out, scale, dshift, y);
+  }
+}
+
+template <typename T, int B>
+int launch_spmm_t(int variant, int64_t rows, const int64_t* ptr, const int32_t* idx, const float* val, const T* in,
+                  T* out, const T* scale, const T* dshift, const T* y, int grid, cudaStream_t s) {
+  switch (variant) {
+    case 0: launch_spmm_v<T, B, 0>(rows, ptr, idx, val, in, out, scale, dshift, y, grid, s); break;
+    case 1: launch_spmm_v<T, B, 1>(rows, ptr, idx, val, in, out, scale, dshift, y, grid, s); break;
+    case 2: launch_spmm_v<T, B, 2>(rows, ptr, idx, val, in, out, scale, dshift, y, grid, s); break;
+    case 3: launch_spmm_v<T, B, 3>(rows, ptr, idx, val, in, out, scale, dshift, y, grid, s); break;
+    case 4: launch_spmm_v<T, B, 4>(rows, ptr, idx, val, in, out, scale, dshift, y, grid, s); break;
+    case 5: launch_spmm_v<T, B, 5>(rows, ptr, idx, val, in, out, scale, dshift, y, grid, s); break;
+    case 6: launch_spmm_v<T, B, 6>(rows, ptr, idx, val, in, out, scale, dshift, y, grid, s); break;
+    case 7: launch_spmm_v<T, B, 7>(rows, ptr, idx, val, in, out, scale, dshift, y, grid, s); break;
+    default: return SG_ERR_ARG;
   }
   return cudaGetLastError() == cudaSuccess ? SG_OK : SG_ERR_CUDA;
 }
 
 template <typename T>
-int launch_spmm(int B, int64_t rows, const int64_t* ptr, const int32_t* idx, const float* val, const T* in,
-                T* out, const T* scale, const T* dshift, const T* y, int grid, cudaStream_t s) {
+int launch_spmm(int variant, int B, int64_t rows, const int64_t* ptr, const int32_t* idx, const float* val,
+                const T* in, T* out, const T* scale, const T* dshift, const T* y, int grid, cudaStream_t s) {
   switch (B) {
-    case 4: return launch_spmm_t<T, 4>(rows, ptr, idx, val, in, out, scale, dshift, y, grid, s);
-    case 8: return launch_spmm_t<T, 8>(rows, ptr, idx, val, in, out, scale, dshift, y, grid, s);
-    case 16: return launch_spmm_t<T, 16>(rows, ptr, idx, val, in, out, scale, dshift, y, grid, s);
-    case 32: return launch_spmm_t<T, 32>(rows, ptr, idx, val, in, out, scale, dshift, y, grid, s);
+    case 4: return launch_spmm_t<T, 4>(variant, rows, ptr, idx, val, in, out, scale, dshift, y, grid, s);
+    case 8: return launch_spmm_t<T, 8>(variant, rows, ptr, idx, val, in, out, scale, dshift, y, grid, s);
+    case 16: return launch_spmm_t<T, 16>(variant, rows, ptr, idx, val, in, out, scale, dshift, y, grid, s);
+    case 32: return launch_spmm_t<T, 32>(variant, rows, ptr, idx, val, in, out, scale, dshift, y, grid, s);
     default: return SG_ERR_ARG;
   }
 }
@@ -422,22 +488,35 @@ extern "C" int sg_csr_select_cols(int64_t n, const int64_t* indptr, const int32_
 
 extern "C" int sg_transpose_blocks(void) { return 2 * sm_count(); }
 
+extern "C" int64_t sg_transpose_work_bytes(int64_t n, int64_t m, int nblk) {
+  if (n < 0 || m <= 0 || nblk <= 0) return -1;
+  const int64_t P = (m + kTrPanel - 1) / kTrPanel;
+  const int64_t cnt = (int64_t)nblk * m * 4;
+  return (cnt + 255) / 256 * 256 + n * (P + 1) * 4;
+}
+
 extern "C" int sg_csr_transpose(int64_t n, int64_t m, const int64_t* indptr, const int32_t* indices,
-                                const float* values, int nblk, int32_t* work, int64_t* colptr,
-                                int32_t* rowidx, float* cvalues, void* scan_scratch, int* status,
-                                void* stream) {
-  if (n < 0 || m <= 0 || nblk <= 0 || m > 0x7fffffffLL || n > 0x7fffffffLL) return SG_ERR_ARG;
+                                const float* values, int nblk, void* work, int64_t work_bytes, int64_t* colptr,
+                                int32_t* rowidx, float* cvalues, void* scan_scratch, int* status, void* stream) {
+  if (n <= 0 || m <= 0 || nblk <= 0 || m > 0x7fffffffLL || n > 0x7fffffffLL) return SG_ERR_ARG;
+  if (work_bytes < sg_transpose_work_bytes(n, m, nblk) || ((uintptr_t)work & 255u)) return SG_ERR_CAP;
   cudaStream_t s = as_stream(stream);
-  if (cudaMemsetAsync(work, 0, (size_t)nblk * (size_t)m * sizeof(int32_t), s) != cudaSuccess) return SG_ERR_CUDA;
-  tr_count<<<nblk, 512, 0, s>>>(n, m, indptr, indices, nblk, work, status);
+  const int P = (int)((m + kTrPanel - 1) / kTrPanel);
+  int32_t* cnt = reinterpret_cast<int32_t*>(work);
+  int32_t* seg = reinterpret_cast<int32_t*>(reinterpret_cast<char*>(work) + ((int64_t)nblk * m * 4 + 255) / 256 * 256);
+  seg_kernel<<<grid_for(n * 32, 256, 8 * sm_count() * 4), 256, 0, s>>>(n, indptr, indices, kTrPanel, P, m, seg,
+                                                                        status);
+  SG_CHECK_LAUNCH();
+  dim3 g2(nblk, P);
+  tr_count<<<g2, 512, 0, s>>>(n, m, indptr, indices, seg, P, nblk, cnt, status);
   SG_CHECK_LAUNCH();
   const int g = grid_for(m, 256, 4096);
-  tr_total<<<g, 256, 0, s>>>(m, nblk, work, colptr);
+  tr_total<<<g, 256, 0, s>>>(m, nblk, cnt, colptr);
   SG_CHECK_LAUNCH();
   if (inclusive_scan_i64(colptr + 1, m, scan_scratch, s) != cudaSuccess) return SG_ERR_CUDA;
-  tr_offsets<<<g, 256, 0, s>>>(m, nblk, work, colptr, nullptr);
+  tr_offsets<<<g, 256, 0, s>>>(m, nblk, cnt);
   SG_CHECK_LAUNCH();
-  tr_fill<<<nblk, kFillBlock, 0, s>>>(n, m, indptr, indices, values, nblk, work, colptr, rowidx, cvalues, status);
+  tr_fill<<<g2, 512, 0, s>>>(n, m, indptr, indices, values, seg, P, nblk, cnt, colptr, rowidx, cvalues, status);
   SG_CHECK_LAUNCH();
   return SG_OK;
 }
@@ -473,18 +552,26 @@ extern "C" int sg_spectral_prepare(int64_t n, int64_t m, const int64_t* indptr, 
   return SG_OK;
 }
 
-extern "C" int sg_spmm(int dtype, int block, int64_t rows, const int64_t* ptr, const int32_t* idx,
-                       const float* val, const void* in, void* out, const void* scale, const void* dshift,
-                       const void* y, int grid, void* stream) {
-  if (rows < 0 || !scale || (dshift && !y)) return SG_ERR_ARG;
+extern "C" int sg_spmm_variants(void) { return kSpmmVariants; }
+
+extern "C" int sg_spmm_ex(int dtype, int block, int64_t rows, const int64_t* ptr, const int32_t* idx,
+                          const float* val, const void* in, void* out, const void* scale, const void* dshift,
+                          const void* y, int grid, int variant, void* stream) {
+  if (rows < 0 || !scale || (dshift && !y) || variant < 0 || variant >= kSpmmVariants) return SG_ERR_ARG;
   if (rows == 0) return SG_OK;
   if (grid <= 0) grid = grid_for(rows * 32, 256, 8 * sm_count() * 4);
   cudaStream_t s = as_stream(stream);
   if (dtype == 0)
-    return launch_spmm<float>(block, rows, ptr, idx, val, (const float*)in, (float*)out, (const float*)scale,
-                              (const float*)dshift, (const float*)y, grid, s);
+    return launch_spmm<float>(variant, block, rows, ptr, idx, val, (const float*)in, (float*)out,
+                              (const float*)scale, (const float*)dshift, (const float*)y, grid, s);
   if (dtype == 1)
-    return launch_spmm<double>(block, rows, ptr, idx, val, (const double*)in, (double*)out,
+    return launch_spmm<double>(variant, block, rows, ptr, idx, val, (const double*)in, (double*)out,
                                (const double*)scale, (const double*)dshift, (const double*)y, grid, s);
   return SG_ERR_ARG;
+}
+
+extern "C" int sg_spmm(int dtype, int block, int64_t rows, const int64_t* ptr, const int32_t* idx,
+                       const float* val, const void* in, void* out, const void* scale, const void* dshift,
+                       const void* y, int grid, void* stream) {
+  return sg_spmm_ex(dtype, block, rows, ptr, idx, val, in, out, scale, dshift, y, grid, 0, stream);
 }

@@ -203,3 +203,56 @@ def test_gpu_spectral_api_and_edges():
     Xz[3, :] = 0
     with pytest.raises(ValueError):
         snap.tl.spectral(snap.AnnData(Xz.tocsr()), features=None)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("valued", [False, True])
+def test_gpu_transpose_matches_scipy(valued):
+    """Deterministic CSR -> CSC: rows ascending within every column, across
+    column panels (m > 16384), with empty rows and empty columns."""
+    import torch
+    from snapatac2_gb300.tools import csr_to_device
+    rng = np.random.default_rng(3)
+    n, m = 3000, 40000
+    X = sp.random(n, m, density=0.002, format="csr", random_state=4)
+    X = X.tolil()
+    X[5, :] = 0
+    X[:, 17000:17100] = 0
+    X = X.tocsr()
+    X.data = rng.integers(1, 9, X.nnz).astype(float) if valued else np.ones(X.nnz)
+    X.sort_indices()
+    from snapatac2_gb300 import _lib
+    L = _lib.load()
+    dev = torch.device("cuda")
+    csr = csr_to_device(X, dev)
+    nblk = int(L.sg_transpose_blocks())
+    wb = int(L.sg_transpose_work_bytes(n, m, nblk))
+    work = torch.empty(wb, dtype=torch.uint8, device=dev)
+    colptr = torch.empty(m + 1, dtype=torch.int64, device=dev)
+    rowidx = torch.empty(X.nnz, dtype=torch.int32, device=dev)
+    cval = torch.empty(X.nnz, dtype=torch.float32, device=dev) if valued else None
+    scan = torch.empty(int(L.sg_scan_scratch_bytes(m + 1)), dtype=torch.uint8, device=dev)
+    st = _lib.DeviceStatus(dev)
+    _lib.check(L.sg_csr_transpose(n, m, csr.indptr.data_ptr(), csr.indices.data_ptr(),
+                                  csr.data.data_ptr() if valued else None, nblk, work.data_ptr(), wb,
+                                  colptr.data_ptr(), rowidx.data_ptr(), cval.data_ptr() if valued else None,
+                                  scan.data_ptr(), st.status_ptr, torch.cuda.current_stream().cuda_stream), "tr")
+    st.raise_if_error("transpose")
+    C = X.tocsc()
+    C.sort_indices()
+    assert np.array_equal(colptr.cpu().numpy(), C.indptr)
+    assert np.array_equal(rowidx.cpu().numpy(), C.indices)
+    if valued:
+        assert np.array_equal(cval.cpu().numpy(), C.data.astype(np.float32))
+
+
+@pytest.mark.gpu
+def test_gpu_rejects_duplicate_columns():
+    import torch
+    from snapatac2_gb300 import _eigen
+    from snapatac2_gb300._binning import DeviceCSR
+    dev = torch.device("cuda")
+    ip = torch.tensor([0, 3, 5], dtype=torch.int64, device=dev)
+    ix = torch.tensor([0, 2, 2, 1, 3], dtype=torch.int32, device=dev)  # row 0 repeats column 2
+    with pytest.raises(ValueError):
+        _eigen.build_operator(DeviceCSR(ip, ix, None, (2, 4)))
