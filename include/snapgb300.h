@@ -217,6 +217,34 @@ int sg_knn(const double* X, int64_t n, int d, int k, int margin, int64_t* nbr, d
            int64_t scratch_bytes, int* n_fallback, void* stream);
 
 /* ------------------------------------------------------------------------ */
+/* Batched Krylov-Schur over many datasets stacked block-diagonally (rows   */
+/* roff[d]..roff[d+1] belong to dataset d).  CTA partition of the rows:     */
+/* cta_r0/cta_r1 (never crossing a dataset), CTAs of dataset d are          */
+/* ds_cta[d]..ds_cta[d+1].  active[d] == 0 freezes dataset d.  C/G/R/H hold */
+/* one block per dataset (strides as documented per call).  No counterpart  */
+/* in the reference, which embeds one dataset per call.                     */
+/* ------------------------------------------------------------------------ */
+int sg_bblock_proj(int dtype, int block, int D, int ncta, const int* ds_cta, const int64_t* cta_r0,
+                   const int64_t* cta_r1, const void* Q, int64_t ldq, int ncols, const void* W, double* part,
+                   double* C, int64_t cstride, void* stream);
+int sg_bblock_update(int dtype, int block, int64_t nrows, int D, const int64_t* roff, const int* active,
+                     const void* Q, int64_t ldq, int ncols, const double* C, int64_t cstride, void* W, void* stream);
+int sg_bblock_cholqr(int dtype, int block, int64_t nrows, int D, const int64_t* roff, const int* active, int ncta,
+                     const int* ds_cta, const int64_t* cta_r0, const int64_t* cta_r1, void* W, double* part,
+                     double* G, double* R, double* Rinv, int* status, int* bad_ds, void* stream);
+int sg_blanczos_hblock(int block, int D, const int* active, double* H, int64_t ldh, int m0, const double* C1,
+                       const double* C2, int64_t cstride, const double* R1, const double* R2, double* Rout,
+                       void* stream);
+int sg_bbasis_rotate(int tq, int to, int ncta, const int* cta_ds, const int64_t* cta_r0, const int64_t* cta_r1,
+                     const void* Q, int64_t ldq, int m, const double* Y, int64_t ldy, int64_t ystride, int k,
+                     void* out, int64_t ldo, void* stream);
+/* Per-dataset IDF on stacked columns (coff column offsets), the rules of   */
+/* idf (snapatac2-python/src/embedding.rs:269-286) with n = the dataset's   */
+/* cell count.  minmax: 2*D uint64 scratch.                                 */
+int sg_bidf(int64_t m, const int64_t* colptr, int D, const int64_t* coff, const int64_t* roff,
+            unsigned long long* minmax, double* w, void* stream);
+
+/* ------------------------------------------------------------------------ */
 /* Adjoint: gradient of the sum of the wanted eigenvalues of the cosine     */
 /* operator with respect to the feature weights (no counterpart in the      */
 /* reference, whose weights are fixed inputs, embedding.rs:42-47).  FP64.   */

@@ -210,19 +210,46 @@ scan_kernel(const TD* __restrict__ Xp, int64_t n, const int* __restrict__ qlist,
   }
 }
 
-// X (n x d FP64) -> padded FP32 / FP64 copies; max row norm (as float bits)
+constexpr int kMeanParts = 256;
+
+// Column means of X (n x d FP64), deterministic: per-CTA partial sums, then a
+// fixed-order reduction.  The FP32 copy is centred on them, which removes the
+// component every point shares and shrinks the FP32 rounding of distances.
+__global__ void mean_partial(const double* __restrict__ X, int64_t n, int d, double* __restrict__ part) {
+  const int b = blockIdx.x, nb = gridDim.x;
+  const int64_t r0 = n * b / nb, r1 = n * (b + 1) / nb;
+  for (int t = threadIdx.x; t < d; t += blockDim.x) {
+    double s = 0.0;
+    for (int64_t i = r0; i < r1; ++i) s += X[i * d + t];
+    part[b * 64 + t] = s;
+  }
+}
+
+__global__ void mean_reduce(const double* __restrict__ part, int nparts, int64_t n, int d, double* __restrict__ mean) {
+  const int t = threadIdx.x;
+  if (t >= 64) return;
+  double s = 0.0;
+  if (t < d)
+    for (int b = 0; b < nparts; ++b) s += part[b * 64 + t];
+  mean[t] = t < d ? s / (double)n : 0.0;
+}
+
+// X -> centred, padded FP32 copy and padded FP64 copy (uncentred: the re-rank
+// uses the reference's arithmetic on the original coordinates); max centred
+// row norm (as float bits, rounded up).
 template <int DP>
-__global__ void prep_kernel(const double* __restrict__ X, int64_t n, int d, float* __restrict__ X32,
-                            double* __restrict__ X64, unsigned* __restrict__ maxnorm_bits) {
+__global__ void prep_kernel(const double* __restrict__ X, int64_t n, int d, const double* __restrict__ mean,
+                            float* __restrict__ X32, double* __restrict__ X64, unsigned* __restrict__ maxnorm_bits) {
   float mx = 0.f;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     double s = 0.0;
 #pragma unroll 4
     for (int t = 0; t < DP; ++t) {
       const double v = t < d ? X[i * d + t] : 0.0;
-      X32[i * DP + t] = (float)v;
+      const double c = t < d ? v - mean[t] : 0.0;
+      X32[i * DP + t] = (float)c;
       X64[i * DP + t] = v;
-      s += v * v;
+      s += c * c;
     }
     mx = fmaxf(mx, (float)sqrt(s) * 1.0000002f);
   }
@@ -251,10 +278,10 @@ __device__ void emit_row(int64_t q, int k, const double* kd, const int* kidx, do
 // FP64 re-rank of the Kp FP32 candidates (warp per query), certificate check.
 template <int DP>
 __global__ void __launch_bounds__(256)
-rerank_kernel(const double* __restrict__ X64, int64_t n, int d, const int* __restrict__ cand, int Kp,
-              const float* __restrict__ tau32, int k, const unsigned* __restrict__ maxnorm_bits,
-              int64_t* __restrict__ nbr, double* __restrict__ dist, int* __restrict__ flagged,
-              int* __restrict__ nflag) {
+rerank_kernel(const double* __restrict__ X64, int64_t n, int d, const double* __restrict__ mean,
+              const int* __restrict__ cand, int Kp, const float* __restrict__ tau32, int k,
+              const unsigned* __restrict__ maxnorm_bits, int64_t* __restrict__ nbr, double* __restrict__ dist,
+              int* __restrict__ flagged, int* __restrict__ nflag) {
   __shared__ double kd[8][kMaxKp];
   __shared__ int kc[8][kMaxKp];
   __shared__ double tk[8][kMaxKp];
@@ -263,8 +290,11 @@ rerank_kernel(const double* __restrict__ X64, int64_t n, int d, const int* __res
   const int64_t q = (int64_t)blockIdx.x * 8 + w;
   if (q >= n) return;
   const double* xq = X64 + q * DP;
-  double qn = 0.0;
-  for (int t = 0; t < d; ++t) qn = fma(xq[t], xq[t], qn);
+  double qn = 0.0;  // centred norm of the query
+  for (int t = 0; t < d; ++t) {
+    const double c = xq[t] - mean[t];
+    qn = fma(c, c, qn);
+  }
   qn = sqrt(qn);
   for (int s = lane; s < kMaxKp; s += 32) {
     const int c = s < Kp ? cand[q * Kp + s] : -1;
@@ -283,16 +313,25 @@ rerank_kernel(const double* __restrict__ X64, int64_t n, int d, const int* __res
   }
   __syncwarp();
   warp_bitonic<double>(kd[w], kc[w], kMaxKp);
-  // Certificate: every point j outside the list has d32(j) >= tau32, and
-  // |d32 - d64| <= delta = (d + 8) * 2^-22 * (|x_q| + max|x|)^2 (rounding of
-  // the inputs to FP32 and of the FP32 sum of squares).
-  const double mx = (double)__uint_as_float(*maxnorm_bits);
-  const double delta = (double)(d + 8) * 2.384185791015625e-07 * (qn + mx) * (qn + mx);
+  // Certificate.  Every point j outside the list has FP32 distance
+  // d32(j) >= tau32.  With u = 2^-24, N = |x_q - mean| + max_j |x_j - mean|
+  // and D the exact squared distance, rounding the centred coordinates to FP32
+  // and the FP32 fused sum of squares give
+  //   |d32 - D| <= 4.1 u N sqrt(D) + (d+1) u D + 5 u^2 N^2,
+  // so every outside point has D >= L, the positive root bound of
+  //   (1 + (d+1)u) s^2 + 4.1 u N s - (tau32 - 5 u^2 N^2) >= 0,  D = s^2.
+  // If L exceeds the k-th FP64 distance among the candidates, the FP64 top-k
+  // is exact.
+  const double u = 5.9604644775390625e-08;
+  const double N = qn + (double)__uint_as_float(*maxnorm_bits);
   const double t32 = (double)tau32[q];
+  const double qa = 1.0 + (double)(d + 1) * u, qb = 4.1 * u * N, qc = t32 - 5.0 * u * u * N * N;
+  const double sroot = qc > 0.0 ? (-qb + sqrt(qb * qb + 4.0 * qa * qc)) / (2.0 * qa) : 0.0;
+  const double lower = sroot * sroot * (1.0 - 4.0 * u);  // absorb the rounding of this bound itself
   const double dk = kd[w][k - 1];
   const bool full = kc[w][k - 1] != 0x7fffffff;
   const bool all_seen = t32 >= 3.0e38;  // fewer than Kp points: every point is a candidate
-  const bool exact = full && (all_seen || t32 - delta > dk);
+  const bool exact = full && (all_seen || lower > dk);
   if (!exact) {
     if (lane == 0) flagged[atomicAdd(nflag, 1)] = (int)q;
     return;
@@ -326,6 +365,8 @@ __global__ void zero_int(int* p, unsigned* u) {
 }
 
 struct KnnScratch {
+  double* mpart;
+  double* mean;
   float* X32;
   double* X64;
   int* cand;
@@ -344,10 +385,13 @@ KnnScratch knn_layout(char* base, int64_t n, int DP, int k, int Kp) {
   KnnScratch s{};
   int64_t o = 0;
   auto take = [&](int64_t b) { int64_t r = o; o += align256(b); return r; };
+  const int64_t omp = take((int64_t)kMeanParts * 64 * 8), omean = take(64 * 8);
   const int64_t oX32 = take(n * DP * 4), oX64 = take(n * DP * 8), oc = take(n * (int64_t)Kp * 4),
                 ot = take(n * 4), of = take(n * 4), ofc = take(n * (int64_t)k * 4),
                 ofd = take(n * (int64_t)k * 8), on = take(16);
   if (base) {
+    s.mpart = (double*)(base + omp);
+    s.mean = (double*)(base + omean);
     s.X32 = (float*)(base + oX32);
     s.X64 = (double*)(base + oX64);
     s.cand = (int*)(base + oc);
@@ -380,12 +424,14 @@ template <int DP>
 int knn_run(const double* X, int64_t n, int d, int k, int Kp, const KnnScratch& w, int64_t* nbr, double* dist,
             cudaStream_t s) {
   zero_int<<<1, 1, 0, s>>>(w.nflag, w.maxnorm);
-  prep_kernel<DP><<<grid_for(n, 256, 4096), 256, 0, s>>>(X, n, d, w.X32, w.X64, w.maxnorm);
+  mean_partial<<<kMeanParts, 64, 0, s>>>(X, n, d, w.mpart);
+  mean_reduce<<<1, 64, 0, s>>>(w.mpart, kMeanParts, n, d, w.mean);
+  prep_kernel<DP><<<grid_for(n, 256, 4096), 256, 0, s>>>(X, n, d, w.mean, w.X32, w.X64, w.maxnorm);
   SG_CHECK_LAUNCH();
   int e = launch_scan<float, DP>(w.X32, n, nullptr, nullptr, Kp, w.cand, nullptr, w.tau32, s);
   if (e) return e;
-  rerank_kernel<DP><<<(unsigned)((n + 7) / 8), 256, 0, s>>>(w.X64, n, d, w.cand, Kp, w.tau32, k, w.maxnorm, nbr,
-                                                            dist, w.flagged, w.nflag);
+  rerank_kernel<DP><<<(unsigned)((n + 7) / 8), 256, 0, s>>>(w.X64, n, d, w.mean, w.cand, Kp, w.tau32, k,
+                                                            w.maxnorm, nbr, dist, w.flagged, w.nflag);
   SG_CHECK_LAUNCH();
   // exact FP64 scan of the rejected queries (CTAs past the count exit at once)
   e = launch_scan<double, DP>(w.X64, n, w.flagged, w.nflag, k, w.fcand, w.fcand_d, nullptr, s);
@@ -449,10 +495,11 @@ constexpr int64_t kNoAllocMaxN = 16384;  // points
 constexpr int kNoAllocMaxDim = 32;       // dimensions
 constexpr int kNoAllocMaxK = 100;        // neighbours
 constexpr int64_t kA256(int64_t x) { return (x + 255) / 256 * 256; }
-// knn_layout(kNoAllocMaxN, 32, kNoAllocMaxK, kMaxKp) written out: X32, X64,
-// candidates, tau, flagged, fallback candidates, fallback distances, counters
+// knn_layout(kNoAllocMaxN, 32, kNoAllocMaxK, kMaxKp) written out: mean partials,
+// mean, X32, X64, candidates, tau, flagged, fallback candidates and
+// distances, counters
 constexpr int64_t kNoAllocBytes =
-    kA256(kNoAllocMaxN * kNoAllocMaxDim * 4) + kA256(kNoAllocMaxN * kNoAllocMaxDim * 8) +
+    kA256((int64_t)kMeanParts * 64 * 8) + kA256(64 * 8) + kA256(kNoAllocMaxN * kNoAllocMaxDim * 4) + kA256(kNoAllocMaxN * kNoAllocMaxDim * 8) +
     kA256(kNoAllocMaxN * kMaxKp * 4) + kA256(kNoAllocMaxN * 4) + kA256(kNoAllocMaxN * 4) +
     kA256(kNoAllocMaxN * kNoAllocMaxK * 4) + kA256(kNoAllocMaxN * kNoAllocMaxK * 8) + kA256(16);
 
