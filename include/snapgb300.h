@@ -163,6 +163,11 @@ int sg_spmm_ex(int dtype, int block, int64_t rows, const int64_t* ptr, const int
                const void* in, void* out, const void* scale, const void* dshift, const void* y, int grid,
                int variant, void* stream);
 
+/* sg_spmm_ex that skips (does not write) the rows with row_mask[r] == 0.    */
+int sg_spmm_masked(int dtype, int block, int64_t rows, const int64_t* ptr, const int32_t* idx, const float* val,
+                   const void* in, void* out, const void* scale, const void* dshift, const void* y, int grid,
+                   int variant, const unsigned char* row_mask, void* stream);
+
 /* ---- block Krylov-Schur (thick-restart block Lanczos) building blocks --- */
 /* Q: n x ldq row-major basis; W: n x block working block.                   */
 
@@ -224,14 +229,17 @@ int sg_knn(const double* X, int64_t n, int d, int k, int margin, int64_t* nbr, d
 /* one block per dataset (strides as documented per call).  No counterpart  */
 /* in the reference, which embeds one dataset per call.                     */
 /* ------------------------------------------------------------------------ */
-int sg_bblock_proj(int dtype, int block, int D, int ncta, const int* ds_cta, const int64_t* cta_r0,
-                   const int64_t* cta_r1, const void* Q, int64_t ldq, int ncols, const void* W, double* part,
-                   double* C, int64_t cstride, void* stream);
+int sg_bblock_proj(int dtype, int block, int D, int ncta, const int* ds_cta, const int* cta_ds, const int* active,
+                   const int64_t* cta_r0, const int64_t* cta_r1, const void* Q, int64_t ldq, int ncols,
+                   const void* W, double* part, double* C, int64_t cstride, void* stream);
 int sg_bblock_update(int dtype, int block, int64_t nrows, int D, const int64_t* roff, const int* active,
                      const void* Q, int64_t ldq, int ncols, const double* C, int64_t cstride, void* W, void* stream);
 int sg_bblock_cholqr(int dtype, int block, int64_t nrows, int D, const int64_t* roff, const int* active, int ncta,
-                     const int* ds_cta, const int64_t* cta_r0, const int64_t* cta_r1, void* W, double* part,
-                     double* G, double* R, double* Rinv, int* status, int* bad_ds, void* stream);
+                     const int* ds_cta, const int* cta_ds, const int64_t* cta_r0, const int64_t* cta_r1, void* W,
+                     double* part, double* G, double* R, double* Rinv, int* status, int* bad_ds, void* stream);
+/* mask[i] = active[d] for the dataset d holding index i (offsets off[D+1]); */
+/* the row masks of sg_spmm_masked for frozen datasets.                      */
+int sg_bmask(int64_t n, int D, const int64_t* off, const int* active, unsigned char* mask, void* stream);
 int sg_blanczos_hblock(int block, int D, const int* active, double* H, int64_t ldh, int m0, const double* C1,
                        const double* C2, int64_t cstride, const double* R1, const double* R2, double* Rout,
                        void* stream);

@@ -116,7 +116,7 @@ class BatchedResult:
 def eigsh_lm_batched(bop: BatchedOperator, k: int, *, precision: str = "mixed", block: int = 8,
                      max_basis: int | None = None, keep: int | None = None, tol_vec: float = 1e-8,
                      tol_val: float = 1e-6, seed: int = 0, max_restarts: int = 200, use_graphs: bool = True,
-                     threads: int = 16) -> BatchedResult:
+                     threads: int = 16, refine: bool = True) -> BatchedResult:
     L = _lib.lib()
     code, tdt = _DT[precision]
     op, D, roff = bop.op, bop.D, bop.roff
@@ -140,7 +140,11 @@ def eigsh_lm_batched(bop: BatchedOperator, k: int, *, precision: str = "mixed", 
     ncta = int(ds_np.shape[0])
     cta_ds, cta_r0, cta_r1, ds_cta = (torch.from_numpy(x).to(dev) for x in (ds_np, r0_np, r1_np, first_np))
     roff_t = torch.from_numpy(roff).to(dev)
+    coff_t = torch.from_numpy(bop.coff).to(dev)
     active = torch.ones(D, dtype=torch.int32, device=dev)
+    # SpMM row masks (cells, features) of frozen datasets
+    op.row_mask = torch.ones(n_tot, dtype=torch.uint8, device=dev)
+    op.col_mask = torch.ones(op.m, dtype=torch.uint8, device=dev)
     cstride = ld * block
     part = torch.empty(ncta * 512 * block, **f64)
     C1, C2 = torch.empty(D * cstride, **f64), torch.empty(D * cstride, **f64)
@@ -154,7 +158,8 @@ def eigsh_lm_batched(bop: BatchedOperator, k: int, *, precision: str = "mixed", 
     def cholqr2(sh):
         for R in (R1, R2):
             chk(L.sg_bblock_cholqr(code, block, n_tot, D, roff_t.data_ptr(), active.data_ptr(), ncta,
-                                   ds_cta.data_ptr(), cta_r0.data_ptr(), cta_r1.data_ptr(), W.data_ptr(),
+                                   ds_cta.data_ptr(), cta_ds.data_ptr(), cta_r0.data_ptr(), cta_r1.data_ptr(),
+                                   W.data_ptr(),
                                    part.data_ptr(), G.data_ptr(), R.data_ptr(), Rinv.data_ptr(), st.status_ptr,
                                    None, sh), "batched cholqr")
 
@@ -164,9 +169,9 @@ def eigsh_lm_batched(bop: BatchedOperator, k: int, *, precision: str = "mixed", 
             op.apply(code, block, Z, Zs, T, W, sh)
             ncols = m + block
             for C in (C1, C2):
-                chk(L.sg_bblock_proj(code, block, D, ncta, ds_cta.data_ptr(), cta_r0.data_ptr(), cta_r1.data_ptr(),
-                                     Q.data_ptr(), ld, ncols, W.data_ptr(), part.data_ptr(), C.data_ptr(), cstride,
-                                     sh), "batched proj")
+                chk(L.sg_bblock_proj(code, block, D, ncta, ds_cta.data_ptr(), cta_ds.data_ptr(), active.data_ptr(),
+                                     cta_r0.data_ptr(), cta_r1.data_ptr(), Q.data_ptr(), ld, ncols, W.data_ptr(),
+                                     part.data_ptr(), C.data_ptr(), cstride, sh), "batched proj")
                 chk(L.sg_bblock_update(code, block, n_tot, D, roff_t.data_ptr(), active.data_ptr(), Q.data_ptr(), ld,
                                        ncols, C.data_ptr(), cstride, W.data_ptr(), sh), "batched update")
             cholqr2(sh)
@@ -198,7 +203,7 @@ def eigsh_lm_batched(bop: BatchedOperator, k: int, *, precision: str = "mixed", 
                 expand(Q, m0, torch.cuda.current_stream(dev).cuda_stream)
             graphs[key] = g
         graphs[key].replay()
-        return M
+        return m0 + (M - m0) // block * block  # where expand() stops
 
     Q, Q2 = Qa, Qb
     m0 = 0
@@ -261,8 +266,11 @@ def eigsh_lm_batched(bop: BatchedOperator, k: int, *, precision: str = "mixed", 
         Q, Q2 = Q2, Q
         H.copy_(torch.from_numpy(Hn))
         active.copy_(torch.from_numpy((~conv).astype(np.int32)))
+        chk(L.sg_bmask(n_tot, D, roff_t.data_ptr(), active.data_ptr(), op.row_mask.data_ptr(), sh0), "mask")
+        chk(L.sg_bmask(op.m, D, coff_t.data_ptr(), active.data_ptr(), op.col_mask.data_ptr(), sh0), "mask")
         m0 = keep
     pool.shutdown()
+    op.row_mask = op.col_mask = None
     Ybuf = np.zeros((D, Me, k))
     ev_out = []
     for d in range(D):
@@ -279,19 +287,70 @@ def eigsh_lm_batched(bop: BatchedOperator, k: int, *, precision: str = "mixed", 
     U = torch.empty(n_tot, k, **f64)
     chk(L.sg_bbasis_rotate(code, 1, ncta, cta_ds.data_ptr(), cta_r0.data_ptr(), cta_r1.data_ptr(), Q.data_ptr(), ld,
                            Me, Yt.data_ptr(), k, Me * k, k, U.data_ptr(), k, sh0), "batched rotate")
+    if refine and precision == "mixed" and k <= 32:
+        ev_out, U = _refine_batched(op, D, k, U, ncta, cta_ds, cta_r0, cta_r1, ds_cta, sh0)
     torch.cuda.synchronize(dev)
     info = dict(block_matvecs=n_mv, restarts=restarts, converged=int(conv.sum()), datasets=D, basis=M, keep=keep,
                 graphs=len(graphs), seconds=time.perf_counter() - t0)
     return BatchedResult(ev_out, U, roff, info)
 
 
-def spectral_batched(mats, n_comps: int = 30, *, precision: str = "mixed", block: int = 8, weighted_by_sd=True,
+def _refine_batched(op, D, k, U, ncta, cta_ds, cta_r0, cta_r1, ds_cta, sh):
+    """FP64 residual-correction sweep of every dataset (see _eigen.fp64_refine):
+    one stacked FP64 SpMM, per-dataset Gram and Rayleigh quotients, host
+    generalized eigenproblems, per-dataset rotation."""
+    L = _lib.load()
+    chk = _lib.check
+    n, dev = op.n, op.a.device
+    kb = 32
+    f64 = dict(dtype=torch.float64, device=dev)
+    Up = torch.zeros(n, kb, **f64)
+    eye = torch.eye(k, dtype=torch.float64).to(dev)
+    chk(L.sg_basis_rotate(1, 1, n, U.data_ptr(), k, k, eye.data_ptr(), k, k, Up.data_ptr(), kb, sh), "copy")
+    part = torch.empty(ncta * kb * kb, **f64)
+    G = torch.empty(D * kb * kb, **f64)
+    Hm = torch.empty(D * kb * kb, **f64)
+    Zs, W = torch.empty(n, kb, **f64), torch.empty(n, kb, **f64)
+    T = torch.empty(op.m, kb, **f64)
+    for Wm, out in ((Up, G), (None, Hm)):
+        if Wm is None:
+            chk(L.sg_block_finish(1, kb, n, Up.data_ptr(), None, 0, 0, None, Zs.data_ptr(), op.a.data_ptr(), sh),
+                "scale")
+            op.apply(1, kb, Up, Zs, T, W, sh)
+            Wm = W
+        chk(L.sg_bblock_proj(1, kb, D, ncta, ds_cta.data_ptr(), cta_ds.data_ptr(), None, cta_r0.data_ptr(),
+                             cta_r1.data_ptr(), Up.data_ptr(), kb, kb, Wm.data_ptr(), part.data_ptr(), out.data_ptr(),
+                             kb * kb, sh), "batched proj")
+    Gh = G.cpu().numpy().reshape(D, kb, kb)[:, :k, :k]
+    Hh = Hm.cpu().numpy().reshape(D, kb, kb)[:, :k, :k]
+    Ybuf = np.zeros((D, kb, k))
+    evs = []
+    for d in range(D):
+        Gk = 0.5 * (Gh[d] + Gh[d].T)
+        Hk = 0.5 * (Hh[d] + Hh[d].T)
+        Ri = np.linalg.inv(np.linalg.cholesky(Gk).T)
+        th, Zr = np.linalg.eigh(Ri.T @ Hk @ Ri)
+        o = np.argsort(-th, kind="stable")
+        Ybuf[d, :k] = (Ri @ Zr)[:, o]
+        evs.append(th[o].copy())
+    Yt = torch.from_numpy(Ybuf).to(dev)
+    Un = torch.empty(n, k, **f64)
+    chk(L.sg_bbasis_rotate(1, 1, ncta, cta_ds.data_ptr(), cta_r0.data_ptr(), cta_r1.data_ptr(), Up.data_ptr(), kb, kb,
+                           Yt.data_ptr(), k, kb * k, k, Un.data_ptr(), k, sh), "batched rotate")
+    return evs, Un
+
+
+def spectral_batched(mats, n_comps: int = 30, *, precision: str = "auto", block: int = 8, weighted_by_sd=True,
                      **kw):
     """Embed many datasets together; returns a list of (evals, X_spectral) per
-    dataset with the same post-processing as ``snap.tl.spectral``."""
-    from .tools import csr_to_device
+    dataset with the same post-processing as ``snap.tl.spectral``.
+    precision='auto' runs FP64 when every dataset is below the single-call
+    threshold (``tools.AUTO_FP64_CELLS``), mixed otherwise."""
+    from .tools import AUTO_FP64_CELLS, csr_to_device
     dev = torch.device("cuda", torch.cuda.current_device())
     mats = [csr_to_device(X, dev) for X in mats]
+    if precision == "auto":
+        precision = "fp64" if max(c.shape[0] for c in mats) < AUTO_FP64_CELLS else "mixed"
     bop = build_batched_operator(mats)
     res = eigsh_lm_batched(bop, n_comps, precision=precision, block=block, **kw)
     out = []

@@ -54,6 +54,8 @@ class GramOperator:
     a32: torch.Tensor
     dinv32: torch.Tensor
     rinv: torch.Tensor | None = None   # FP64 1/||(XW)_i|| (kept for the adjoint)
+    row_mask: torch.Tensor | None = None  # uint8 per cell: 0 skips the row (frozen batched datasets)
+    col_mask: torch.Tensor | None = None  # uint8 per feature
     timings: dict = field(default_factory=dict)
     variants: dict = field(default_factory=dict)  # (dtype, block) -> (Xᵀ pass, X pass)
 
@@ -73,14 +75,16 @@ class GramOperator:
         if ev is not None:
             e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
             e0.record()
-        _lib.check(L.sg_spmm_ex(dtype_code, block, self.m, self.colptr.data_ptr(), self.rowidx.data_ptr(), cv,
-                                Zs.data_ptr(), T.data_ptr(), w2.data_ptr(), None, None, -1, vt, stream),
+        cm = self.col_mask.data_ptr() if self.col_mask is not None else None
+        rm = self.row_mask.data_ptr() if self.row_mask is not None else None
+        _lib.check(L.sg_spmm_masked(dtype_code, block, self.m, self.colptr.data_ptr(), self.rowidx.data_ptr(), cv,
+                                    Zs.data_ptr(), T.data_ptr(), w2.data_ptr(), None, None, -1, vt, cm, stream),
                    "sg_spmm (Xᵀ)")
         if ev is not None:
             e1.record()
-        _lib.check(L.sg_spmm_ex(dtype_code, block, self.n, self.csr.indptr.data_ptr(), self.csr.indices.data_ptr(),
-                                v, T.data_ptr(), W.data_ptr(), a.data_ptr(), dinv.data_ptr(), Z.data_ptr(), -1, vx,
-                                stream), "sg_spmm (X)")
+        _lib.check(L.sg_spmm_masked(dtype_code, block, self.n, self.csr.indptr.data_ptr(),
+                                    self.csr.indices.data_ptr(), v, T.data_ptr(), W.data_ptr(), a.data_ptr(),
+                                    dinv.data_ptr(), Z.data_ptr(), -1, vx, rm, stream), "sg_spmm (X)")
         if ev is not None:
             e2.record()
             ev.append((e0, e1, e2, self, dtype_code, block))
@@ -104,6 +108,10 @@ def tune_spmm(op: "GramOperator", code: int, block: int, Z, Zs, T, W, stream: in
         vt, vx = (int(x) for x in forced.split(","))
         op.variants[(code, block)] = (vt, vx)
         return vt, vx
+    if code == 1:  # FP64 form: deeper unroll only where registers allow it
+        res = (2, 2) if block <= 8 else (0, 0)
+        op.variants[(code, block)] = res
+        return res
     key = (code, block, op.n, op.m, op.csr.nnz >> 20, op.csr.data is not None)
     if key in _TUNED:
         op.variants[(code, block)] = _TUNED[key]
@@ -276,7 +284,8 @@ def _default_basis(k: int, block: int, n: int) -> tuple[int, int]:
 
 def eigsh_lm(op: GramOperator, k: int, *, precision: str = "mixed", block: int = 8, max_basis: int | None = None,
              keep: int | None = None, tol_vec: float = 1e-8, tol_val: float = 1e-6, vec_positive_only: bool = True,
-             seed: int = 0, max_restarts: int = 200, stream: torch.cuda.Stream | None = None) -> EigenResult:
+             seed: int = 0, max_restarts: int = 200, stream: torch.cuda.Stream | None = None,
+             refine: bool = True) -> EigenResult:
     """k eigenpairs of largest magnitude (ARPACK ``which='LM'``) of ``op``.
 
     Convergence: every wanted Ritz pair must have ||A y - θ y|| <= tol·max|θ|,
@@ -393,12 +402,62 @@ def eigsh_lm(op: GramOperator, k: int, *, precision: str = "mixed", block: int =
     U = torch.empty(n, k, **f64)
     _lib.check(L.sg_basis_rotate(code, 1, n, Q.data_ptr(), ld, Me, Yk.data_ptr(), k, k, U.data_ptr(), k, sh),
                "rotate")
+    evals = th[sel].copy()
+    if refine and precision == "mixed" and k <= 32:
+        evals, U = fp64_refine(op, U, k, sh)
     torch.cuda.synchronize(dev)
     beyond = order[k:k + 4]  # Ritz values just outside the wanted set
     info = dict(block_matvecs=n_mv, vector_matvecs=n_mv * block, restarts=restarts, basis=M, keep=keep,
                 residuals=res[sel].tolist(), converged=worst <= 1.0, seconds=time.perf_counter() - t0,
                 precision=precision, block=block, next_evals=th[beyond].tolist())
-    return EigenResult(th[sel].copy(), U, info)
+    return EigenResult(evals, U, info)
+
+
+def fp64_refine(op: GramOperator, U: torch.Tensor, k: int, stream: int):
+    """Final FP64 residual-correction sweep of mixed-precision Ritz pairs.
+
+    U (n x k, FP64) spans the converged FP32 Ritz vectors.  One FP64 block
+    matvec A U (FP64 SpMM, block 32) and FP64 Rayleigh-Ritz on span(U)
+    (Gram matrix G = UᵀU, H = Uᵀ A U, generalized eigenproblem H y = θ G y by
+    Cholesky) give eigenvalues with error O(angle²), i.e. at FP64 level, and
+    re-rotate the vectors inside the subspace.  Returns (θ descending, U').
+    """
+    L = _lib.load()
+    n, dev = op.n, op.a.device
+    kb = 32
+    if k > kb:
+        raise ValueError("refinement supports k <= 32")
+    f64 = dict(dtype=torch.float64, device=dev)
+    Up = torch.zeros(n, kb, **f64)
+    eye = torch.eye(k, dtype=torch.float64).to(dev)
+    _lib.check(L.sg_basis_rotate(1, 1, n, U.data_ptr(), k, k, eye.data_ptr(), k, k, Up.data_ptr(), kb, stream),
+               "copy")
+    nparts = int(L.sg_proj_parts())
+    part = torch.empty(nparts * kb * kb, **f64)
+    G = torch.empty(kb * kb, **f64)
+    Hm = torch.empty(kb * kb, **f64)
+    Zs, W = torch.empty(n, kb, **f64), torch.empty(n, kb, **f64)
+    T = torch.empty(op.m, kb, **f64)
+    _lib.check(L.sg_block_proj(1, kb, n, Up.data_ptr(), kb, kb, Up.data_ptr(), part.data_ptr(), nparts,
+                               G.data_ptr(), stream), "gram")
+    _lib.check(L.sg_block_finish(1, kb, n, Up.data_ptr(), None, 0, 0, None, Zs.data_ptr(), op.a.data_ptr(), stream),
+               "scale")
+    op.apply(1, kb, Up, Zs, T, W, stream)
+    _lib.check(L.sg_block_proj(1, kb, n, Up.data_ptr(), kb, kb, W.data_ptr(), part.data_ptr(), nparts,
+                               Hm.data_ptr(), stream), "rayleigh quotient")
+    Gk = G.cpu().numpy().reshape(kb, kb)[:k, :k]
+    Hk = Hm.cpu().numpy().reshape(kb, kb)[:k, :k]
+    Hk = 0.5 * (Hk + Hk.T)
+    Rc = np.linalg.cholesky(0.5 * (Gk + Gk.T)).T      # G = Rᵀ R
+    Ri = np.linalg.inv(Rc)
+    th, Zr = np.linalg.eigh(Ri.T @ Hk @ Ri)
+    Y = Ri @ Zr
+    order = np.argsort(-th, kind="stable")
+    Yt = torch.from_numpy(np.ascontiguousarray(Y[:, order])).to(dev)
+    Un = torch.empty(n, k, **f64)
+    _lib.check(L.sg_basis_rotate(1, 1, n, Up.data_ptr(), kb, k, Yt.data_ptr(), k, k, Un.data_ptr(), k, stream),
+               "rotate")
+    return th[order].copy(), Un
 
 
 def _dense_small(op: GramOperator, k: int, code: int, tdt, block: int) -> EigenResult:

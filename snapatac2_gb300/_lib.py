@@ -59,9 +59,12 @@ SIGNATURES: dict[str, tuple] = {
     "sg_knn_scratch_bytes": (_I64, [_I64, _I32, _I32, _I32]),
     "sg_knn": (_I32, [_P, _I64, _I32, _I32, _I32, _P, _P, _P, _I64, _P, _P]),
     "sg_knn_noalloc": (_I32, [_P, _I64, _I32, _I32, _I32, _P, _P, _P, _P]),
-    "sg_bblock_proj": (_I32, [_I32, _I32, _I32, _I32, _P, _P, _P, _P, _I64, _I32, _P, _P, _P, _I64, _P]),
+    "sg_bblock_proj": (_I32, [_I32, _I32, _I32, _I32, _P, _P, _P, _P, _P, _P, _I64, _I32, _P, _P, _P, _I64, _P]),
+    "sg_bmask": (_I32, [_I64, _I32, _P, _P, _P, _P]),
+    "sg_spmm_masked": (_I32, [_I32, _I32, _I64, _P, _P, _P, _P, _P, _P, _P, _P, _I32, _I32, _P, _P]),
     "sg_bblock_update": (_I32, [_I32, _I32, _I64, _I32, _P, _P, _P, _I64, _I32, _P, _I64, _P, _P]),
-    "sg_bblock_cholqr": (_I32, [_I32, _I32, _I64, _I32, _P, _P, _I32, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
+    "sg_bblock_cholqr": (_I32, [_I32, _I32, _I64, _I32, _P, _P, _I32, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P,
+                                _P]),
     "sg_blanczos_hblock": (_I32, [_I32, _I32, _P, _P, _I64, _I32, _P, _P, _I64, _P, _P, _P, _P]),
     "sg_bbasis_rotate": (_I32, [_I32, _I32, _I32, _P, _P, _P, _P, _I64, _I32, _P, _I64, _I64, _I32, _P, _I64, _P]),
     "sg_bidf": (_I32, [_I64, _P, _I32, _P, _P, _P, _P, _P]),
@@ -80,9 +83,12 @@ KERNELS_PER_CALL = {
     "sg_tile_plan": 4, "sg_tile_run": 5, "sg_tile_emit": 1, "sg_csr_select_cols": 5,
     "sg_csr_transpose": 8, "sg_spectral_prepare": 7, "sg_spmm": 1, "sg_spmm_ex": 1, "sg_block_proj": 2,
     "sg_block_update": 1, "sg_block_cholqr": 4, "sg_block_finish": 1, "sg_lanczos_hblock": 1,
-    "sg_bblock_proj": (_I32, [_I32, _I32, _I32, _I32, _P, _P, _P, _P, _I64, _I32, _P, _P, _P, _I64, _P]),
+    "sg_bblock_proj": (_I32, [_I32, _I32, _I32, _I32, _P, _P, _P, _P, _P, _P, _I64, _I32, _P, _P, _P, _I64, _P]),
+    "sg_bmask": (_I32, [_I64, _I32, _P, _P, _P, _P]),
+    "sg_spmm_masked": (_I32, [_I32, _I32, _I64, _P, _P, _P, _P, _P, _P, _P, _P, _I32, _I32, _P, _P]),
     "sg_bblock_update": (_I32, [_I32, _I32, _I64, _I32, _P, _P, _P, _I64, _I32, _P, _I64, _P, _P]),
-    "sg_bblock_cholqr": (_I32, [_I32, _I32, _I64, _I32, _P, _P, _I32, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
+    "sg_bblock_cholqr": (_I32, [_I32, _I32, _I64, _I32, _P, _P, _I32, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P,
+                                _P]),
     "sg_blanczos_hblock": (_I32, [_I32, _I32, _P, _P, _I64, _I32, _P, _P, _I64, _P, _P, _P, _P]),
     "sg_bbasis_rotate": (_I32, [_I32, _I32, _I32, _P, _P, _P, _P, _I64, _I32, _P, _I64, _I64, _I32, _P, _I64, _P]),
     "sg_bidf": (_I32, [_I64, _P, _I32, _P, _P, _P, _P, _P]),
@@ -93,6 +99,7 @@ KERNELS_PER_CALL = {
     "sg_square_values": (_I32, [_I64, _P, _P, _P]),
     "sg_basis_rotate": 1, "sg_fill_random": 1, "sg_knn": 6, "sg_adjoint_stage1": 1, "sg_bblock_proj": 2, "sg_bblock_update": 1,
     "sg_bblock_cholqr": 4, "sg_blanczos_hblock": 1, "sg_bbasis_rotate": 1, "sg_bidf": 3,
+    "sg_bmask": 1, "sg_spmm_masked": 1,
     "sg_adjoint_stage2": 1, "sg_adjoint_stage3": 1, "sg_adjoint_final": 1, "sg_square_values": 1,
 }
 

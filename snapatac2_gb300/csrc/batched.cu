@@ -35,10 +35,12 @@ __device__ __forceinline__ int find_ds(const int64_t* roff_s, int D, int64_t i) 
 
 template <typename T, int B, int CPT>
 __global__ void __launch_bounds__(256)
-bproj_partial(const int64_t* __restrict__ cta_r0, const int64_t* __restrict__ cta_r1, const T* __restrict__ Q,
-              int64_t ldq, int ncols, const T* __restrict__ W, double* __restrict__ part) {
+bproj_partial(const int64_t* __restrict__ cta_r0, const int64_t* __restrict__ cta_r1, const int* __restrict__ cta_ds,
+              const int* __restrict__ active, const T* __restrict__ Q, int64_t ldq, int ncols,
+              const T* __restrict__ W, double* __restrict__ part) {
   __shared__ T ws[32][B];
   const int b = blockIdx.x;
+  if (active && !active[cta_ds[b]]) return;  // frozen dataset: its C is not used
   const int64_t r0 = cta_r0[b], r1 = cta_r1[b];
   T acc[CPT][B];
 #pragma unroll
@@ -264,12 +266,13 @@ int nsm() {
 }
 
 template <typename T, int B>
-int bproj_t(int ncta, const int64_t* r0, const int64_t* r1, const int* ds_cta, int D, const T* Q, int64_t ldq,
-            int ncols, const T* W, double* part, double* C, int64_t cstride, cudaStream_t s) {
+int bproj_t(int ncta, const int64_t* r0, const int64_t* r1, const int* cta_ds, const int* active, const int* ds_cta,
+            int D, const T* Q, int64_t ldq, int ncols, const T* W, double* part, double* C, int64_t cstride,
+            cudaStream_t s) {
   for (int c0 = 0; c0 < ncols; c0 += 512) {
     const int nc = ncols - c0 < 512 ? ncols - c0 : 512;
-    if (nc <= 256) bproj_partial<T, B, 1><<<ncta, 256, 0, s>>>(r0, r1, Q + c0, ldq, nc, W, part);
-    else bproj_partial<T, B, 2><<<ncta, 256, 0, s>>>(r0, r1, Q + c0, ldq, nc, W, part);
+    if (nc <= 256) bproj_partial<T, B, 1><<<ncta, 256, 0, s>>>(r0, r1, cta_ds, active, Q + c0, ldq, nc, W, part);
+    else bproj_partial<T, B, 2><<<ncta, 256, 0, s>>>(r0, r1, cta_ds, active, Q + c0, ldq, nc, W, part);
     SG_CHECK_LAUNCH();
     const int tot = nc * B;
     dim3 g((tot + 255) / 256, D);
@@ -294,24 +297,42 @@ using namespace sg;
   }
 
 template <typename T>
-static int bproj_any(int block, int ncta, const int64_t* r0, const int64_t* r1, const int* ds_cta, int D,
-                     const T* Q, int64_t ldq, int ncols, const T* W, double* part, double* C, int64_t cstride,
-                     cudaStream_t s) {
-  SG_BDISPATCH(bproj_t, ncta, r0, r1, ds_cta, D, Q, ldq, ncols, W, part, C, cstride, s)
+static int bproj_any(int block, int ncta, const int64_t* r0, const int64_t* r1, const int* cta_ds, const int* active,
+                     const int* ds_cta, int D, const T* Q, int64_t ldq, int ncols, const T* W, double* part, double* C,
+                     int64_t cstride, cudaStream_t s) {
+  SG_BDISPATCH(bproj_t, ncta, r0, r1, cta_ds, active, ds_cta, D, Q, ldq, ncols, W, part, C, cstride, s)
 }
 
-extern "C" int sg_bblock_proj(int dtype, int block, int D, int ncta, const int* ds_cta, const int64_t* cta_r0,
-                              const int64_t* cta_r1, const void* Q, int64_t ldq, int ncols, const void* W,
-                              double* part, double* C, int64_t cstride, void* stream) {
+extern "C" int sg_bblock_proj(int dtype, int block, int D, int ncta, const int* ds_cta, const int* cta_ds,
+                              const int* active, const int64_t* cta_r0, const int64_t* cta_r1, const void* Q,
+                              int64_t ldq, int ncols, const void* W, double* part, double* C, int64_t cstride,
+                              void* stream) {
   if (D <= 0 || D > kMaxDatasets || ncta <= 0 || ncols <= 0 || cstride < (int64_t)ncols * block) return SG_ERR_ARG;
   cudaStream_t s = as_stream(stream);
   if (dtype == 0)
-    return bproj_any<float>(block, ncta, cta_r0, cta_r1, ds_cta, D, (const float*)Q, ldq, ncols, (const float*)W,
-                            part, C, cstride, s);
+    return bproj_any<float>(block, ncta, cta_r0, cta_r1, cta_ds, active, ds_cta, D, (const float*)Q, ldq, ncols,
+                            (const float*)W, part, C, cstride, s);
   if (dtype == 1)
-    return bproj_any<double>(block, ncta, cta_r0, cta_r1, ds_cta, D, (const double*)Q, ldq, ncols,
+    return bproj_any<double>(block, ncta, cta_r0, cta_r1, cta_ds, active, ds_cta, D, (const double*)Q, ldq, ncols,
                              (const double*)W, part, C, cstride, s);
   return SG_ERR_ARG;
+}
+
+// mask[i] = active[dataset of i] for i < n (offsets off[D+1]).
+__global__ void bmask_kernel(int64_t n, int D, const int64_t* __restrict__ off, const int* __restrict__ active,
+                             unsigned char* __restrict__ mask) {
+  __shared__ int64_t off_s[kMaxDatasets + 1];
+  for (int t = threadIdx.x; t <= D; t += blockDim.x) off_s[t] = off[t];
+  __syncthreads();
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    mask[i] = active[find_ds(off_s, D, i)] ? 1 : 0;
+}
+
+extern "C" int sg_bmask(int64_t n, int D, const int64_t* off, const int* active, unsigned char* mask, void* stream) {
+  if (n <= 0 || D <= 0 || D > kMaxDatasets) return SG_ERR_ARG;
+  bmask_kernel<<<grid_for(n, 256, 8 * nsm()), 256, 0, as_stream(stream)>>>(n, D, off, active, mask);
+  SG_CHECK_LAUNCH();
+  return SG_OK;
 }
 
 extern "C" int sg_bblock_update(int dtype, int block, int64_t nrows, int D, const int64_t* roff, const int* active,
@@ -339,11 +360,11 @@ extern "C" int sg_bblock_update(int dtype, int block, int64_t nrows, int D, cons
 
 // One batched Cholesky-QR pass over every dataset's block.
 extern "C" int sg_bblock_cholqr(int dtype, int block, int64_t nrows, int D, const int64_t* roff, const int* active,
-                                int ncta, const int* ds_cta, const int64_t* cta_r0, const int64_t* cta_r1, void* W,
-                                double* part, double* G, double* R, double* Rinv, int* status, int* bad_ds,
-                                void* stream) {
+                                int ncta, const int* ds_cta, const int* cta_ds, const int64_t* cta_r0,
+                                const int64_t* cta_r1, void* W, double* part, double* G, double* R, double* Rinv,
+                                int* status, int* bad_ds, void* stream) {
   if (block < 1 || block > 32) return SG_ERR_ARG;
-  int e = sg_bblock_proj(dtype, block, D, ncta, ds_cta, cta_r0, cta_r1, W, block, block, W, part, G,
+  int e = sg_bblock_proj(dtype, block, D, ncta, ds_cta, cta_ds, active, cta_r0, cta_r1, W, block, block, W, part, G,
                          (int64_t)block * block, stream);
   if (e) return e;
   cudaStream_t s = as_stream(stream);

@@ -73,6 +73,53 @@ proj_partial(int64_t n, const T* __restrict__ Q, int64_t ldq, int ncols, const T
   }
 }
 
+// Gram partials of a block: part[blk][i*B + j] = sum over this CTA's rows of
+// W[r,i] W[r,j].  Thread per row (all threads busy, unlike the projection
+// kernel with only B basis columns); upper triangle in registers, then a
+// fixed-order reduction over the CTA's threads (deterministic).
+template <typename T, int B>
+__global__ void __launch_bounds__(256) gram_partial(int64_t n, const T* __restrict__ W, double* __restrict__ part) {
+  constexpr int NT = B * (B + 1) / 2;
+  __shared__ double red[256 / 32][NT];
+  const int nb = gridDim.x, b = blockIdx.x;
+  const int64_t r0 = n * b / nb, r1 = n * (b + 1) / nb;
+  T acc[NT];
+#pragma unroll
+  for (int t = 0; t < NT; ++t) acc[t] = T(0);
+  for (int64_t r = r0 + threadIdx.x; r < r1; r += 256) {
+    T w[B];
+#pragma unroll
+    for (int i = 0; i < B; ++i) w[i] = W[r * B + i];
+    int t = 0;
+#pragma unroll
+    for (int i = 0; i < B; ++i)
+#pragma unroll
+      for (int j = i; j < B; ++j) {
+        acc[t] = fma(w[i], w[j], acc[t]);
+        ++t;
+      }
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int t = 0; t < NT; ++t) {
+    double v = (double)acc[t];
+#pragma unroll
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) red[wid][t] = v;
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < NT; t += 256) {
+    double v = 0.0;
+    for (int w2 = 0; w2 < 256 / 32; ++w2) v += red[w2][t];
+    // position t -> (i, j) of the packed upper triangle
+    int i = 0, rem = t;
+    while (rem >= B - i) { rem -= B - i; ++i; }
+    const int j = i + rem;
+    part[(int64_t)b * B * B + i * B + j] = v;
+    part[(int64_t)b * B * B + j * B + i] = v;
+  }
+}
+
 __global__ void proj_reduce(int nparts, int ncols, int B, const double* __restrict__ part, double* __restrict__ C) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int tot = ncols * B;
@@ -370,9 +417,19 @@ extern "C" int sg_block_update(int dtype, int block, int64_t n, const void* Q, i
 extern "C" int sg_block_cholqr(int dtype, int block, int64_t n, void* W, double* part, int nparts, double* G,
                                double* R, double* Rinv, int* status, void* stream) {
   if (n <= 0 || block < 1 || block > 32) return SG_ERR_ARG;
-  int e = sg_block_proj(dtype, block, n, W, block, block, W, part, nparts, G, stream);
-  if (e) return e;
   cudaStream_t s = as_stream(stream);
+  int e = SG_OK;
+  if (dtype == 0 && block == 8) gram_partial<float, 8><<<nparts, 256, 0, s>>>(n, (const float*)W, part);
+  else if (dtype == 0 && block == 4) gram_partial<float, 4><<<nparts, 256, 0, s>>>(n, (const float*)W, part);
+  else if (dtype == 1 && block == 8) gram_partial<double, 8><<<nparts, 256, 0, s>>>(n, (const double*)W, part);
+  else if (dtype == 1 && block == 4) gram_partial<double, 4><<<nparts, 256, 0, s>>>(n, (const double*)W, part);
+  else e = sg_block_proj(dtype, block, n, W, block, block, W, part, nparts, G, stream);
+  if (e) return e;
+  if (block == 4 || block == 8) {
+    SG_CHECK_LAUNCH();
+    proj_reduce<<<(block * block + 255) / 256, 256, 0, s>>>(nparts, block, block, part, G);
+    SG_CHECK_LAUNCH();
+  }
   chol_kernel<<<1, 32, 0, s>>>(block, G, R, Rinv, status);
   SG_CHECK_LAUNCH();
   if (dtype == 0) return rinv_dispatch<float>(block, n, Rinv, (float*)W, s);

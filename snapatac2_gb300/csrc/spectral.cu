@@ -351,7 +351,8 @@ template <typename T, int B, bool VALUED, bool SHIFT, int VAR>
 __global__ void __launch_bounds__(256)
 spmm_kernel(int64_t rows, const int64_t* __restrict__ ptr, const int32_t* __restrict__ idx,
             const float* __restrict__ val, const T* __restrict__ in, T* __restrict__ out,
-            const T* __restrict__ scale, const T* __restrict__ dshift, const T* __restrict__ y) {
+            const T* __restrict__ scale, const T* __restrict__ dshift, const T* __restrict__ y,
+            const unsigned char* __restrict__ row_mask) {
   using VT = typename V16<T>::type;
   constexpr int VW = V16<T>::n;
   constexpr int LPN = B / VW;          // lanes per nonzero
@@ -365,6 +366,7 @@ spmm_kernel(int64_t rows, const int64_t* __restrict__ ptr, const int32_t* __rest
   const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
   for (int64_t r = gw; r < rows; r += nw) {
+    if (row_mask && !row_mask[r]) continue;  // frozen row (warp-uniform)
     const int64_t s = ptr[r], e = ptr[r + 1];
     VT acc = V16<T>::zero();
     for (int64_t base = s; base < e; base += 32 * CH) {
@@ -419,28 +421,29 @@ constexpr int kSpmmVariants = 8;
 
 template <typename T, int B, int VAR>
 void launch_spmm_v(int64_t rows, const int64_t* ptr, const int32_t* idx, const float* val, const T* in, T* out,
-                   const T* scale, const T* dshift, const T* y, int grid, cudaStream_t s) {
+                   const T* scale, const T* dshift, const T* y, int grid, cudaStream_t s, const unsigned char* mk) {
   if (val) {
-    if (dshift) spmm_kernel<T, B, true, true, VAR><<<grid, 256, 0, s>>>(rows, ptr, idx, val, in, out, scale, dshift, y);
-    else spmm_kernel<T, B, true, false, VAR><<<grid, 256, 0, s>>>(rows, ptr, idx, val, in, out, scale, dshift, y);
+    if (dshift) spmm_kernel<T, B, true, true, VAR><<<grid, 256, 0, s>>>(rows, ptr, idx, val, in, out, scale, dshift, y, mk);
+    else spmm_kernel<T, B, true, false, VAR><<<grid, 256, 0, s>>>(rows, ptr, idx, val, in, out, scale, dshift, y, mk);
   } else {
-    if (dshift) spmm_kernel<T, B, false, true, VAR><<<grid, 256, 0, s>>>(rows, ptr, idx, val, in, out, scale, dshift, y);
-    else spmm_kernel<T, B, false, false, VAR><<<grid, 256, 0, s>>>(rows, ptr, idx, val, in, out, scale, dshift, y);
+    if (dshift) spmm_kernel<T, B, false, true, VAR><<<grid, 256, 0, s>>>(rows, ptr, idx, val, in, out, scale, dshift, y, mk);
+    else spmm_kernel<T, B, false, false, VAR><<<grid, 256, 0, s>>>(rows, ptr, idx, val, in, out, scale, dshift, y, mk);
   }
 }
 
 template <typename T, int B>
 int launch_spmm_t(int variant, int64_t rows, const int64_t* ptr, const int32_t* idx, const float* val, const T* in,
-                  T* out, const T* scale, const T* dshift, const T* y, int grid, cudaStream_t s) {
+                  T* out, const T* scale, const T* dshift, const T* y, int grid, cudaStream_t s,
+                  const unsigned char* mk) {
   switch (variant) {
-    case 0: launch_spmm_v<T, B, 0>(rows, ptr, idx, val, in, out, scale, dshift, y, grid, s); break;
-    case 1: launch_spmm_v<T, B, 1>(rows, ptr, idx, val, in, out, scale, dshift, y, grid, s); break;
-    case 2: launch_spmm_v<T, B, 2>(rows, ptr, idx, val, in, out, scale, dshift, y, grid, s); break;
-    case 3: launch_spmm_v<T, B, 3>(rows, ptr, idx, val, in, out, scale, dshift, y, grid, s); break;
-    case 4: launch_spmm_v<T, B, 4>(rows, ptr, idx, val, in, out, scale, dshift, y, grid, s); break;
-    case 5: launch_spmm_v<T, B, 5>(rows, ptr, idx, val, in, out, scale, dshift, y, grid, s); break;
-    case 6: launch_spmm_v<T, B, 6>(rows, ptr, idx, val, in, out, scale, dshift, y, grid, s); break;
-    case 7: launch_spmm_v<T, B, 7>(rows, ptr, idx, val, in, out, scale, dshift, y, grid, s); break;
+    case 0: launch_spmm_v<T, B, 0>(rows, ptr, idx, val, in, out, scale, dshift, y, grid, s, mk); break;
+    case 1: launch_spmm_v<T, B, 1>(rows, ptr, idx, val, in, out, scale, dshift, y, grid, s, mk); break;
+    case 2: launch_spmm_v<T, B, 2>(rows, ptr, idx, val, in, out, scale, dshift, y, grid, s, mk); break;
+    case 3: launch_spmm_v<T, B, 3>(rows, ptr, idx, val, in, out, scale, dshift, y, grid, s, mk); break;
+    case 4: launch_spmm_v<T, B, 4>(rows, ptr, idx, val, in, out, scale, dshift, y, grid, s, mk); break;
+    case 5: launch_spmm_v<T, B, 5>(rows, ptr, idx, val, in, out, scale, dshift, y, grid, s, mk); break;
+    case 6: launch_spmm_v<T, B, 6>(rows, ptr, idx, val, in, out, scale, dshift, y, grid, s, mk); break;
+    case 7: launch_spmm_v<T, B, 7>(rows, ptr, idx, val, in, out, scale, dshift, y, grid, s, mk); break;
     default: return SG_ERR_ARG;
   }
   return cudaGetLastError() == cudaSuccess ? SG_OK : SG_ERR_CUDA;
@@ -448,12 +451,13 @@ int launch_spmm_t(int variant, int64_t rows, const int64_t* ptr, const int32_t* 
 
 template <typename T>
 int launch_spmm(int variant, int B, int64_t rows, const int64_t* ptr, const int32_t* idx, const float* val,
-                const T* in, T* out, const T* scale, const T* dshift, const T* y, int grid, cudaStream_t s) {
+                const T* in, T* out, const T* scale, const T* dshift, const T* y, int grid, cudaStream_t s,
+                const unsigned char* mk) {
   switch (B) {
-    case 4: return launch_spmm_t<T, 4>(variant, rows, ptr, idx, val, in, out, scale, dshift, y, grid, s);
-    case 8: return launch_spmm_t<T, 8>(variant, rows, ptr, idx, val, in, out, scale, dshift, y, grid, s);
-    case 16: return launch_spmm_t<T, 16>(variant, rows, ptr, idx, val, in, out, scale, dshift, y, grid, s);
-    case 32: return launch_spmm_t<T, 32>(variant, rows, ptr, idx, val, in, out, scale, dshift, y, grid, s);
+    case 4: return launch_spmm_t<T, 4>(variant, rows, ptr, idx, val, in, out, scale, dshift, y, grid, s, mk);
+    case 8: return launch_spmm_t<T, 8>(variant, rows, ptr, idx, val, in, out, scale, dshift, y, grid, s, mk);
+    case 16: return launch_spmm_t<T, 16>(variant, rows, ptr, idx, val, in, out, scale, dshift, y, grid, s, mk);
+    case 32: return launch_spmm_t<T, 32>(variant, rows, ptr, idx, val, in, out, scale, dshift, y, grid, s, mk);
     default: return SG_ERR_ARG;
   }
 }
@@ -554,20 +558,26 @@ extern "C" int sg_spectral_prepare(int64_t n, int64_t m, const int64_t* indptr, 
 
 extern "C" int sg_spmm_variants(void) { return kSpmmVariants; }
 
-extern "C" int sg_spmm_ex(int dtype, int block, int64_t rows, const int64_t* ptr, const int32_t* idx,
-                          const float* val, const void* in, void* out, const void* scale, const void* dshift,
-                          const void* y, int grid, int variant, void* stream) {
+extern "C" int sg_spmm_masked(int dtype, int block, int64_t rows, const int64_t* ptr, const int32_t* idx,
+                              const float* val, const void* in, void* out, const void* scale, const void* dshift,
+                              const void* y, int grid, int variant, const unsigned char* row_mask, void* stream) {
   if (rows < 0 || !scale || (dshift && !y) || variant < 0 || variant >= kSpmmVariants) return SG_ERR_ARG;
   if (rows == 0) return SG_OK;
   if (grid <= 0) grid = grid_for(rows * 32, 256, 8 * sm_count() * 4);
   cudaStream_t s = as_stream(stream);
   if (dtype == 0)
     return launch_spmm<float>(variant, block, rows, ptr, idx, val, (const float*)in, (float*)out,
-                              (const float*)scale, (const float*)dshift, (const float*)y, grid, s);
+                              (const float*)scale, (const float*)dshift, (const float*)y, grid, s, row_mask);
   if (dtype == 1)
     return launch_spmm<double>(variant, block, rows, ptr, idx, val, (const double*)in, (double*)out,
-                               (const double*)scale, (const double*)dshift, (const double*)y, grid, s);
+                               (const double*)scale, (const double*)dshift, (const double*)y, grid, s, row_mask);
   return SG_ERR_ARG;
+}
+
+extern "C" int sg_spmm_ex(int dtype, int block, int64_t rows, const int64_t* ptr, const int32_t* idx,
+                          const float* val, const void* in, void* out, const void* scale, const void* dshift,
+                          const void* y, int grid, int variant, void* stream) {
+  return sg_spmm_masked(dtype, block, rows, ptr, idx, val, in, out, scale, dshift, y, grid, variant, nullptr, stream);
 }
 
 extern "C" int sg_spmm(int dtype, int block, int64_t rows, const int64_t* ptr, const int32_t* idx,

@@ -18,6 +18,10 @@ from . import _eigen
 from ._binning import DeviceCSR
 
 
+# Below this many cells precision='auto' runs the all-FP64 form.
+AUTO_FP64_CELLS = 20_000
+
+
 def _device(device=None) -> torch.device:
     if device is not None:
         return torch.device(device)
@@ -86,15 +90,18 @@ def spectral(
     feature_weights: list[float] | None = None,
     inplace: bool = True,
     *,
-    precision: Literal["mixed", "fp64"] = "mixed",
+    precision: Literal["auto", "mixed", "fp64"] = "auto",
     block: int = 8,
     device=None,
 ):
     """Laplacian-eigenmap embedding (``_embedding.py:129-295``), cosine, full sample.
 
-    Extra keywords: ``precision`` ('mixed': FP32 SpMM and basis with FP64
-    Rayleigh-Ritz; 'fp64': all FP64), ``block`` (Lanczos block size),
-    ``device``.
+    Extra keywords: ``precision`` ('mixed': FP32 SpMM and basis, FP64
+    Rayleigh-Ritz and a final FP64 correction sweep; 'fp64': all FP64;
+    'auto' (default): FP64 below ``AUTO_FP64_CELLS`` cells, where it is cheap
+    and where the top eigenvalues reach into a dense bulk whose gaps are
+    comparable to the FP32 noise floor, mixed above), ``block`` (Lanczos
+    block size), ``device``.
     """
     np.random.seed(random_state)
     if isinstance(features, str):
@@ -119,6 +126,8 @@ def spectral(
     if distance_metric != "cosine":
         raise NotImplementedError("only distance_metric='cosine' (matrix-free) is supported")
 
+    if precision == "auto":
+        precision = "fp64" if adata.n_obs < AUTO_FP64_CELLS else "mixed"
     evals, evecs = spectral_embedding(adata.X, features, n_comps, random_state, feature_weights,
                                       precision=precision, block=block, device=device)
     if weighted_by_sd:
