@@ -33,6 +33,7 @@ extern "C" {
 #define SG_ERR_CAP 3      /* caller-provided buffer too small */
 #define SG_ERR_CUDA 4     /* a CUDA launch or runtime call failed */
 #define SG_ERR_NUMERIC 5  /* numerical breakdown (e.g. non-positive Gram pivot) */
+#define SG_ERR_TIMEOUT 6  /* a bounded device-side wait gave up (copy never completed) */
 
 /* Counting strategies, same meaning as CountingStrategy in
  * snapatac2-core/src/feature_count/counter.rs:19-36 ("insertion", "fragment",
@@ -167,6 +168,26 @@ int sg_spmm_ex(int dtype, int block, int64_t rows, const int64_t* ptr, const int
 int sg_spmm_masked(int dtype, int block, int64_t rows, const int64_t* ptr, const int32_t* idx, const float* val,
                    const void* in, void* out, const void* scale, const void* dshift, const void* y, int grid,
                    int variant, const unsigned char* row_mask, void* stream);
+
+/* Stage-tiled SpMM, same result contract as sg_spmm_masked (summation     */
+/* order differs at rounding level).  One CTA per SM (and wave) owns a row  */
+/* range; the dense operand `in` (cols x block, every row is read) streams  */
+/* through shared memory in column stages by bulk asynchronous copies,      */
+/* together with each stage's segment table (per row: the [start, end) of   */
+/* its nonzeros in the stage), built once by sg_staged_table for the matrix */
+/* and the (dtype, block) row width.  in/out/y/table 16-byte aligned; out   */
+/* must not alias in.  A stage copy that never completes sets               */
+/* *status = SG_ERR_TIMEOUT (bounded 2 s wait).  Variants in                */
+/* [0, sg_spmm_staged_variants()) differ in lanes per row and unroll.        */
+int sg_spmm_staged_variants(void);
+/* Bytes of the segment table for this shape (0: shape not supported).      */
+int64_t sg_staged_table_bytes(int dtype, int block, int64_t rows, int64_t cols);
+int sg_staged_table(int dtype, int block, int64_t rows, int64_t cols, const int64_t* ptr, const int32_t* idx,
+                    void* table, int64_t table_bytes, void* stream);
+int sg_spmm_staged(int dtype, int block, int64_t rows, int64_t cols, const int64_t* ptr, const int32_t* idx,
+                   const float* val, const void* table, const void* in, void* out, const void* scale,
+                   const void* dshift, const void* y, int variant, const unsigned char* row_mask, int* status,
+                   void* stream);
 
 /* ---- block Krylov-Schur (thick-restart block Lanczos) building blocks --- */
 /* Q: n x ldq row-major basis; W: n x block working block.                   */

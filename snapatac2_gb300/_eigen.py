@@ -58,6 +58,8 @@ class GramOperator:
     col_mask: torch.Tensor | None = None  # uint8 per feature
     timings: dict = field(default_factory=dict)
     variants: dict = field(default_factory=dict)  # (dtype, block) -> (Xᵀ pass, X pass)
+    status: object = None  # DeviceStatus of the staged SpMM's bounded waits (created on first use)
+    staged_tables: dict = field(default_factory=dict)  # (pass, row bytes) -> segment table (uint8)
 
     def scales(self, dtype_code: int):
         if dtype_code == 0:
@@ -66,41 +68,87 @@ class GramOperator:
 
     def apply(self, dtype_code: int, block: int, Z, Zs, T, W, stream: int) -> None:
         """W = A Z (Zs = a ⊙ Z precomputed); T is m x block scratch."""
-        L = _lib.load()
-        w2, a, dinv = self.scales(dtype_code)
-        cv = self.cvalues.data_ptr() if self.cvalues is not None else None
-        v = self.csr.data.data_ptr() if self.csr.data is not None else None
         vt, vx = self.variants.get((dtype_code, block)) or tune_spmm(self, dtype_code, block, Z, Zs, T, W, stream)
         ev = SPMM_EVENTS
         if ev is not None:
             e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
             e0.record()
-        cm = self.col_mask.data_ptr() if self.col_mask is not None else None
-        rm = self.row_mask.data_ptr() if self.row_mask is not None else None
-        _lib.check(L.sg_spmm_masked(dtype_code, block, self.m, self.colptr.data_ptr(), self.rowidx.data_ptr(), cv,
-                                    Zs.data_ptr(), T.data_ptr(), w2.data_ptr(), None, None, -1, vt, cm, stream),
-                   "sg_spmm (Xᵀ)")
+        self.spmm_pass(0, vt, dtype_code, block, Zs, T, stream)
         if ev is not None:
             e1.record()
-        _lib.check(L.sg_spmm_masked(dtype_code, block, self.n, self.csr.indptr.data_ptr(),
-                                    self.csr.indices.data_ptr(), v, T.data_ptr(), W.data_ptr(), a.data_ptr(),
-                                    dinv.data_ptr(), Z.data_ptr(), -1, vx, rm, stream), "sg_spmm (X)")
+        self.spmm_pass(1, vx, dtype_code, block, T, W, stream, Z)
         if ev is not None:
             e2.record()
             ev.append((e0, e1, e2, self, dtype_code, block))
 
+    def spmm_pass(self, which: int, variant: int, dtype_code: int, block: int, inp, out, stream: int,
+                  y=None) -> int:
+        """One SpMM launch: which = 0 is T = w² ⊙ Xᵀ inp (CSC, rows = features),
+        which = 1 is out = a ⊙ X inp - dinv ⊙ y (CSR, rows = cells).  Variants
+        below STAGED select the gather kernel (sg_spmm_masked), STAGED + v
+        the stage-tiled kernel (sg_spmm_staged).  Returns the C status."""
+        L = _lib.load()
+        w2, a, dinv = self.scales(dtype_code)
+        if which == 0:
+            rows, cols, ptr, idx = self.m, self.n, self.colptr, self.rowidx
+            val = self.cvalues.data_ptr() if self.cvalues is not None else None
+            scale, dsh, yp = w2.data_ptr(), None, None
+            mask = self.col_mask.data_ptr() if self.col_mask is not None else None
+        else:
+            rows, cols, ptr, idx = self.n, self.m, self.csr.indptr, self.csr.indices
+            val = self.csr.data.data_ptr() if self.csr.data is not None else None
+            scale, dsh, yp = a.data_ptr(), dinv.data_ptr(), y.data_ptr()
+            mask = self.row_mask.data_ptr() if self.row_mask is not None else None
+        if variant >= STAGED:
+            if self.status is None:
+                self.status = _lib.DeviceStatus(self.a.device)
+            table = self.staged_table(which, dtype_code, block, stream)
+            rc = L.sg_spmm_staged(dtype_code, block, rows, cols, ptr.data_ptr(), idx.data_ptr(), val,
+                                  table.data_ptr(), inp.data_ptr(), out.data_ptr(), scale, dsh, yp,
+                                  variant - STAGED, mask, self.status.status_ptr, stream)
+        else:
+            rc = L.sg_spmm_masked(dtype_code, block, rows, ptr.data_ptr(), idx.data_ptr(), val, inp.data_ptr(),
+                                  out.data_ptr(), scale, dsh, yp, -1, variant, mask, stream)
+        _lib.check(rc, "sg_spmm (Xᵀ)" if which == 0 else "sg_spmm (X)")
+        return rc
+
+
+    def staged_table(self, which: int, dtype_code: int, block: int, stream: int) -> torch.Tensor:
+        """Segment table of the stage-tiled SpMM for one pass, built once per
+        row width (block x element size) and kept with the operator."""
+        key = (which, block * (4 if dtype_code == 0 else 8))
+        t = self.staged_tables.get(key)
+        if t is None:
+            L = _lib.load()
+            rows, cols = (self.m, self.n) if which == 0 else (self.n, self.m)
+            ptr, idx = (self.colptr, self.rowidx) if which == 0 else (self.csr.indptr, self.csr.indices)
+            nb = int(L.sg_staged_table_bytes(dtype_code, block, rows, cols))
+            if nb <= 0:
+                raise _lib.SnapGB300Error(_lib.SG_ERR_ARG, "staged SpMM: shape not supported")
+            t = torch.empty(nb, dtype=torch.uint8, device=self.a.device)
+            _lib.check(L.sg_staged_table(dtype_code, block, rows, cols, ptr.data_ptr(), idx.data_ptr(),
+                                         t.data_ptr(), nb, stream), "sg_staged_table")
+            self.staged_tables[key] = t
+        return t
+
+
+# Variant codes >= STAGED select the stage-tiled SpMM kernel.
+STAGED = 100
 
 _TUNED: dict = {}
 
 
 def tune_spmm(op: "GramOperator", code: int, block: int, Z, Zs, T, W, stream: int) -> tuple[int, int]:
-    """Pick the fastest SpMM memory-access variant for each pass.
+    """Pick the fastest SpMM kernel and variant for each pass.
 
-    Every variant computes the same result; each is timed (CUDA events, one
+    Candidates: the gather kernel's memory-access variants (same arithmetic,
+    same result) and the stage-tiled kernel's variants (same sums in another
+    order: rounding-level differences).  Each is timed (CUDA events, one
     warm-up launch + two timed) on this operator's matrices with zero-filled
-    block buffers of the caller's shapes as operands.  The choice is cached per process for the
-    shape class (dtype, block, n, m, nnz in units of 2^20, valued) and can be
-    forced with SNAPGB300_SPMM_VARIANT=<t>,<x>.
+    block buffers of the caller's shapes as operands.  The choice is cached
+    per process for the shape class (dtype, block, n, m, nnz in units of
+    2^20, valued, masked) and can be forced with
+    SNAPGB300_SPMM_VARIANT=<t>,<x> (codes >= 100 select the staged kernel).
     """
     import os
     forced = os.environ.get("SNAPGB300_SPMM_VARIANT")
@@ -108,31 +156,27 @@ def tune_spmm(op: "GramOperator", code: int, block: int, Z, Zs, T, W, stream: in
         vt, vx = (int(x) for x in forced.split(","))
         op.variants[(code, block)] = (vt, vx)
         return vt, vx
-    if code == 1:  # FP64 form: deeper unroll only where registers allow it
-        res = (2, 2) if block <= 8 else (0, 0)
-        op.variants[(code, block)] = res
-        return res
-    key = (code, block, op.n, op.m, op.csr.nnz >> 20, op.csr.data is not None)
+    key = (code, block, op.n, op.m, op.csr.nnz >> 20, op.csr.data is not None, op.row_mask is not None)
     if key in _TUNED:
         op.variants[(code, block)] = _TUNED[key]
         return _TUNED[key]
     L = _lib.load()
-    nvar = int(L.sg_spmm_variants())
-    w2, a, dinv = op.scales(code)
-    cv = op.cvalues.data_ptr() if op.cvalues is not None else None
-    v = op.csr.data.data_ptr() if op.csr.data is not None else None
+    gather = list(range(int(L.sg_spmm_variants())))
+    if code == 1 and block > 8:  # FP64 wide blocks: the deeper unrolls spill
+        gather = [v for v in gather if (v & 3) < 2]
+    cands = gather + [STAGED + v for v in range(int(L.sg_spmm_staged_variants()))]
     # private operands: the caller's blocks hold live solver state
     Z, Zs, T, W = (torch.zeros_like(t) for t in (Z, Zs, T, W))
 
     def time_pass(which: int, var: int) -> float:
         def launch():
             if which == 0:
-                return L.sg_spmm_ex(code, block, op.m, op.colptr.data_ptr(), op.rowidx.data_ptr(), cv, Zs.data_ptr(),
-                                    T.data_ptr(), w2.data_ptr(), None, None, -1, var, stream)
-            return L.sg_spmm_ex(code, block, op.n, op.csr.indptr.data_ptr(), op.csr.indices.data_ptr(), v,
-                                T.data_ptr(), W.data_ptr(), a.data_ptr(), dinv.data_ptr(), Z.data_ptr(), -1, var,
-                                stream)
-        _lib.check(launch(), "sg_spmm_ex (tuning)")
+                return op.spmm_pass(0, var, code, block, Zs, T, stream)
+            return op.spmm_pass(1, var, code, block, T, W, stream, Z)
+        try:
+            launch()
+        except _lib.SnapGB300Error:
+            return math.inf  # shape not supported by this variant
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
         for _ in range(2):
@@ -143,9 +187,14 @@ def tune_spmm(op: "GramOperator", code: int, block: int, Z, Zs, T, W, stream: in
 
     best = []
     for which in (0, 1):
-        times = [time_pass(which, var) for var in range(nvar)]
-        best.append(int(np.argmin(times)))
+        times = [time_pass(which, var) for var in cands]
+        best.append(cands[int(np.argmin(times))])
+    if op.status is not None:
+        op.status.raise_if_error("staged SpMM")
     res = (best[0], best[1])
+    for which in (0, 1):  # tables of passes that did not pick the staged kernel
+        if res[which] < STAGED:
+            op.staged_tables.pop((which, block * (4 if code == 0 else 8)), None)
     _TUNED[key] = res
     op.variants[(code, block)] = res
     return res

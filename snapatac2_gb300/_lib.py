@@ -22,6 +22,7 @@ SG_ERR_RANGE = 2
 SG_ERR_CAP = 3
 SG_ERR_CUDA = 4
 SG_ERR_NUMERIC = 5
+SG_ERR_TIMEOUT = 6
 
 _P = ctypes.c_void_p
 _I64 = ctypes.c_int64
@@ -62,6 +63,10 @@ SIGNATURES: dict[str, tuple] = {
     "sg_bblock_proj": (_I32, [_I32, _I32, _I32, _I32, _P, _P, _P, _P, _P, _P, _I64, _I32, _P, _P, _P, _I64, _P]),
     "sg_bmask": (_I32, [_I64, _I32, _P, _P, _P, _P]),
     "sg_spmm_masked": (_I32, [_I32, _I32, _I64, _P, _P, _P, _P, _P, _P, _P, _P, _I32, _I32, _P, _P]),
+    "sg_spmm_staged_variants": (_I32, []),
+    "sg_staged_table_bytes": (_I64, [_I32, _I32, _I64, _I64]),
+    "sg_staged_table": (_I32, [_I32, _I32, _I64, _I64, _P, _P, _P, _I64, _P]),
+    "sg_spmm_staged": (_I32, [_I32, _I32, _I64, _I64, _P, _P, _P, _P, _P, _P, _P, _P, _P, _I32, _P, _P, _P]),
     "sg_bblock_update": (_I32, [_I32, _I32, _I64, _I32, _P, _P, _P, _I64, _I32, _P, _I64, _P, _P]),
     "sg_bblock_cholqr": (_I32, [_I32, _I32, _I64, _I32, _P, _P, _I32, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P,
                                 _P]),
@@ -81,26 +86,13 @@ SIGNATURES: dict[str, tuple] = {
 # R⁻¹ application.
 KERNELS_PER_CALL = {
     "sg_tile_plan": 4, "sg_tile_run": 5, "sg_tile_emit": 1, "sg_csr_select_cols": 5,
-    "sg_csr_transpose": 8, "sg_spectral_prepare": 7, "sg_spmm": 1, "sg_spmm_ex": 1, "sg_block_proj": 2,
-    "sg_block_update": 1, "sg_block_cholqr": 4, "sg_block_finish": 1, "sg_lanczos_hblock": 1,
-    "sg_bblock_proj": (_I32, [_I32, _I32, _I32, _I32, _P, _P, _P, _P, _P, _P, _I64, _I32, _P, _P, _P, _I64, _P]),
-    "sg_bmask": (_I32, [_I64, _I32, _P, _P, _P, _P]),
-    "sg_spmm_masked": (_I32, [_I32, _I32, _I64, _P, _P, _P, _P, _P, _P, _P, _P, _I32, _I32, _P, _P]),
-    "sg_bblock_update": (_I32, [_I32, _I32, _I64, _I32, _P, _P, _P, _I64, _I32, _P, _I64, _P, _P]),
-    "sg_bblock_cholqr": (_I32, [_I32, _I32, _I64, _I32, _P, _P, _I32, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P,
-                                _P]),
-    "sg_blanczos_hblock": (_I32, [_I32, _I32, _P, _P, _I64, _I32, _P, _P, _I64, _P, _P, _P, _P]),
-    "sg_bbasis_rotate": (_I32, [_I32, _I32, _I32, _P, _P, _P, _P, _I64, _I32, _P, _I64, _I64, _I32, _P, _I64, _P]),
-    "sg_bidf": (_I32, [_I64, _P, _I32, _P, _P, _P, _P, _P]),
-    "sg_adjoint_stage1": (_I32, [_I64, _I32, _P, _P, _P, _P, _I32, _P, _P, _P]),
-    "sg_adjoint_stage2": (_I32, [_I64, _I32, _P, _I32, _P, _I32, _P, _P]),
-    "sg_adjoint_stage3": (_I32, [_I64, _I32, _P, _P, _P, _P, _P, _I32, _P, _P]),
-    "sg_adjoint_final": (_I32, [_I64, _I32, _P, _P, _I32, _P, _P, _P]),
-    "sg_square_values": (_I32, [_I64, _P, _P, _P]),
-    "sg_basis_rotate": 1, "sg_fill_random": 1, "sg_knn": 6, "sg_adjoint_stage1": 1, "sg_bblock_proj": 2, "sg_bblock_update": 1,
-    "sg_bblock_cholqr": 4, "sg_blanczos_hblock": 1, "sg_bbasis_rotate": 1, "sg_bidf": 3,
-    "sg_bmask": 1, "sg_spmm_masked": 1,
-    "sg_adjoint_stage2": 1, "sg_adjoint_stage3": 1, "sg_adjoint_final": 1, "sg_square_values": 1,
+    "sg_csr_transpose": 8, "sg_spectral_prepare": 7, "sg_spmm": 1, "sg_spmm_ex": 1, "sg_spmm_masked": 1,
+    "sg_spmm_staged": 1, "sg_staged_table": 1, "sg_block_proj": 2, "sg_block_update": 1, "sg_block_cholqr": 4, "sg_block_finish": 1,
+    "sg_lanczos_hblock": 1, "sg_basis_rotate": 1, "sg_fill_random": 1, "sg_knn": 6, "sg_knn_noalloc": 6,
+    "sg_bblock_proj": 2, "sg_bblock_update": 1, "sg_bblock_cholqr": 4, "sg_blanczos_hblock": 1,
+    "sg_bbasis_rotate": 1, "sg_bidf": 3, "sg_bmask": 1,
+    "sg_adjoint_stage1": 1, "sg_adjoint_stage2": 1, "sg_adjoint_stage3": 1, "sg_adjoint_final": 1,
+    "sg_square_values": 1,
 }
 
 _lock = threading.Lock()

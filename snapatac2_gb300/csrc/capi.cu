@@ -11,6 +11,7 @@ extern "C" const char* sg_status_string(int status) {
     case SG_ERR_CAP: return "buffer too small";
     case SG_ERR_CUDA: return "CUDA error";
     case SG_ERR_NUMERIC: return "numerical breakdown";
+    case SG_ERR_TIMEOUT: return "device-side wait timed out";
     default: return "unknown status";
   }
 }

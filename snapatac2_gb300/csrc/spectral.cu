@@ -313,31 +313,6 @@ __global__ void square_weights(int64_t m, const double* __restrict__ w, double* 
 // (one coalesced 128-byte load) and broadcast by shuffles.  Partial sums are
 // combined by a fixed xor-shuffle tree: results are deterministic.
 // ---------------------------------------------------------------------------
-template <typename T> struct V16;
-template <> struct V16<float> {
-  using type = float4;
-  static constexpr int n = 4;
-  __device__ static float4 zero() { return make_float4(0.f, 0.f, 0.f, 0.f); }
-  __device__ static void add(float4& a, const float4& b) { a.x += b.x; a.y += b.y; a.z += b.z; a.w += b.w; }
-  __device__ static void fma(float4& a, float s, const float4& b) {
-    a.x = fmaf(s, b.x, a.x); a.y = fmaf(s, b.y, a.y); a.z = fmaf(s, b.z, a.z); a.w = fmaf(s, b.w, a.w);
-  }
-  __device__ static float4 shfl_xor(const float4& v, int o) {
-    return make_float4(__shfl_xor_sync(0xffffffffu, v.x, o), __shfl_xor_sync(0xffffffffu, v.y, o),
-                       __shfl_xor_sync(0xffffffffu, v.z, o), __shfl_xor_sync(0xffffffffu, v.w, o));
-  }
-};
-template <> struct V16<double> {
-  using type = double2;
-  static constexpr int n = 2;
-  __device__ static double2 zero() { return make_double2(0.0, 0.0); }
-  __device__ static void add(double2& a, const double2& b) { a.x += b.x; a.y += b.y; }
-  __device__ static void fma(double2& a, double s, const double2& b) { a.x = ::fma(s, b.x, a.x); a.y = ::fma(s, b.y, a.y); }
-  __device__ static double2 shfl_xor(const double2& v, int o) {
-    return make_double2(__shfl_xor_sync(0xffffffffu, v.x, o), __shfl_xor_sync(0xffffffffu, v.y, o));
-  }
-};
-
 // Variants (same arithmetic, same result, picked by the autotuner): bits 0-1
 // select 1, 2, 4 or 8 chunks of 32 column indices in flight per iteration
 // (more gathers outstanding per lane against fewer resident warps); bit 2

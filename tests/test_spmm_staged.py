@@ -1,0 +1,118 @@
+"""Stage-tiled SpMM (sg_staged_table + sg_spmm_staged) against an FP64 NumPy product.
+
+out[r] = scale[r] * sum_e val_e * in[col_e]  - dshift[r] * y[r]; rows with
+row_mask 0 are not written.  Shapes cover one and many operand stages, the
+shared-memory and the L2 accumulator paths, more rows than one wave of CTAs
+holds, empty rows and valued matrices.  FP32 within 2e-6 relative of the
+row's absolute sum, FP64 within 1e-13.
+"""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+from snapatac2_gb300 import _lib
+
+
+def random_csr(rows, cols, per_row, seed, valued):
+    rng = np.random.default_rng(seed)
+    nnz_row = rng.poisson(per_row, rows)
+    nnz_row[rng.random(rows) < 0.05] = 0  # empty rows
+    row_of = np.repeat(np.arange(rows, dtype=np.int64), nnz_row)
+    keys = np.unique(row_of * cols + rng.integers(0, cols, row_of.size))  # sorted, unique per row
+    indptr = np.zeros(rows + 1, np.int64)
+    np.cumsum(np.bincount(keys // cols, minlength=rows), out=indptr[1:])
+    idx = (keys % cols).astype(np.int32)
+    val = rng.integers(1, 5, idx.size).astype(np.float32) if valued else None
+    return indptr, idx, val
+
+
+CASES = [
+    # rows, cols, nnz/row, dtype, block, valued, shift, masked
+    (3000, 500, 20, 0, 8, False, True, False),        # one stage
+    (5000, 60000, 40, 0, 8, False, True, False),      # many stages, smem accumulators
+    (5000, 60000, 40, 0, 8, True, False, True),       # valued + mask
+    (4000, 30000, 30, 0, 4, False, True, False),
+    (4000, 30000, 30, 0, 16, True, True, False),
+    (3000, 20000, 30, 0, 32, False, True, True),      # wide rows: L2 accumulators
+    (4000, 30000, 30, 1, 8, False, True, False),      # FP64
+    (3000, 12000, 30, 1, 32, True, True, False),
+    (330000, 9000, 3, 0, 8, False, True, False),      # accumulators beyond 64 KB per CTA -> L2
+    (1300000, 2000, 2, 0, 8, False, False, False),    # more than one wave of CTAs
+]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("rows,cols,per_row,dtype,block,valued,shift,masked", CASES)
+def test_staged_spmm_matches_fp64(rows, cols, per_row, dtype, block, valued, shift, masked):
+    import torch
+    L = _lib.lib()
+    dev = torch.device("cuda", 0)
+    tdt = torch.float32 if dtype == 0 else torch.float64
+    indptr, idx, val = random_csr(rows, cols, per_row, rows + cols + block, valued)
+    rng = np.random.default_rng(7)
+    inp = rng.standard_normal((cols, block))
+    scale = rng.uniform(0.5, 2.0, rows)
+    dsh = rng.uniform(0.1, 1.0, rows) if shift else None
+    y = rng.standard_normal((rows, block)) if shift else None
+    mask = (rng.random(rows) < 0.7).astype(np.uint8) if masked else None
+    # reference (FP64) on the values the kernel sees
+    cast = (lambda a: a.astype(np.float32).astype(np.float64)) if dtype == 0 else (lambda a: a)
+    X = sp.csr_matrix((val.astype(np.float64) if valued else np.ones(idx.size), idx, indptr), shape=(rows, cols))
+    absX = abs(X)
+    ref = cast(scale)[:, None] * (X @ cast(inp))
+    bound = cast(scale)[:, None] * (absX @ np.abs(cast(inp)))
+    if shift:
+        ref -= cast(dsh)[:, None] * cast(y)
+        bound += np.abs(cast(dsh)[:, None] * cast(y))
+    t = lambda a, dt=tdt: torch.from_numpy(np.ascontiguousarray(a)).to(dev, dt)  # noqa: E731
+    d_ptr, d_idx = t(indptr, torch.int64), t(idx, torch.int32)
+    d_val = t(val, torch.float32) if valued else None
+    d_in, d_scale = t(inp), t(scale)
+    d_dsh, d_y = (t(dsh), t(y)) if shift else (None, None)
+    d_mask = t(mask, torch.uint8) if masked else None
+    sentinel = 12345.0
+    out = torch.full((rows, block), sentinel, dtype=tdt, device=dev)
+    st = _lib.DeviceStatus(dev)
+    sh = torch.cuda.current_stream(dev).cuda_stream
+    p = lambda x: None if x is None else x.data_ptr()  # noqa: E731
+    nb = int(L.sg_staged_table_bytes(dtype, block, rows, cols))
+    assert nb > 0
+    table = torch.empty(nb, dtype=torch.uint8, device=dev)
+    assert L.sg_staged_table(dtype, block, rows, cols, d_ptr.data_ptr(), d_idx.data_ptr(), table.data_ptr(),
+                             nb - 16, sh) == _lib.SG_ERR_CAP
+    assert L.sg_staged_table(dtype, block, rows, cols, d_ptr.data_ptr(), d_idx.data_ptr(), table.data_ptr(),
+                             nb, sh) == _lib.SG_OK
+    for v in range(int(L.sg_spmm_staged_variants())):
+        out.fill_(sentinel)
+        rc = L.sg_spmm_staged(dtype, block, rows, cols, d_ptr.data_ptr(), d_idx.data_ptr(), p(d_val),
+                              table.data_ptr(), d_in.data_ptr(), out.data_ptr(), d_scale.data_ptr(), p(d_dsh),
+                              p(d_y), v, p(d_mask), st.status_ptr, sh)
+        assert rc == _lib.SG_OK, (v, rc)
+        st.raise_if_error("staged SpMM")
+        got = out.cpu().numpy().astype(np.float64)
+        live = np.ones(rows, bool) if mask is None else mask.astype(bool)
+        assert np.all(got[~live] == sentinel), "masked rows were written"
+        tol = (2e-6 if dtype == 0 else 1e-13) * (bound[live] + 1e-30)
+        err = np.abs(got[live] - ref[live])
+        assert np.all(err <= tol), (v, float(np.max(err / (bound[live] + 1e-30))))
+
+
+@pytest.mark.gpu
+def test_staged_spmm_rejects_bad_arguments():
+    import torch
+    L = _lib.lib()
+    dev = torch.device("cuda", 0)
+    ptr = torch.zeros(3, dtype=torch.int64, device=dev)
+    idx = torch.zeros(1, dtype=torch.int32, device=dev)
+    buf = torch.zeros(64, dtype=torch.float32, device=dev)
+    st = _lib.DeviceStatus(dev)
+    sh = torch.cuda.current_stream(dev).cuda_stream
+    table = torch.zeros(4096, dtype=torch.uint8, device=dev)
+    args = lambda cols, variant, inp: (0, 8, 2, cols, ptr.data_ptr(), idx.data_ptr(), None,  # noqa: E731
+                                       table.data_ptr(), inp, buf.data_ptr(), buf.data_ptr(), None, None, variant,
+                                       None, st.status_ptr, sh)
+    assert L.sg_staged_table_bytes(0, 8, 2, 0) == 0                                 # no columns
+    assert L.sg_staged_table_bytes(0, 12, 2, 2) == 0                                # no such block
+    assert L.sg_spmm_staged(*args(0, 0, buf.data_ptr())) == _lib.SG_ERR_ARG        # no columns
+    assert L.sg_spmm_staged(*args(2, 99, buf.data_ptr())) == _lib.SG_ERR_ARG       # no such variant
+    assert L.sg_spmm_staged(*args(2, 0, buf.data_ptr() + 4)) == _lib.SG_ERR_ARG    # misaligned operand
