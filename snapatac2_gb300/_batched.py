@@ -35,6 +35,7 @@ class BatchedOperator:
     roff: np.ndarray          # int64 [D+1] row offsets
     coff: np.ndarray          # int64 [D+1] column offsets
     op: _eigen.GramOperator   # on the stacked matrix
+    timings: dict | None = None  # seconds of the build phases
 
 
 def stack(mats: list[DeviceCSR]) -> tuple[DeviceCSR, np.ndarray, np.ndarray]:
@@ -62,33 +63,49 @@ def stack(mats: list[DeviceCSR]) -> tuple[DeviceCSR, np.ndarray, np.ndarray]:
 
 
 def build_batched_operator(mats: list[DeviceCSR]) -> BatchedOperator:
+    """Stacked operator of the datasets.  The CSC of the block-diagonal stack
+    is the concatenation of the datasets' own CSCs (row indices offset by the
+    dataset's first row, column pointers by its first nonzero), so each
+    dataset is transposed on its own: a transpose of the stack would walk
+    every row once per 16,384-column panel of all datasets together."""
     L = _lib.lib()
+    dev = mats[0].indptr.device
+    tm = {}
+    t0 = time.perf_counter()
     S, roff, coff = stack(mats)
-    dev = S.indptr.device
+    torch.cuda.synchronize(dev)
+    tm["stack"] = time.perf_counter() - t0
     D = len(mats)
-    # transpose first to get column counts, then per-dataset IDF weights
     n, m = S.shape
-    st = _lib.DeviceStatus(dev)
     sh = torch.cuda.current_stream(dev).cuda_stream
-    nblk = max(1, min(int(L.sg_transpose_blocks()), n))
-    wb = int(L.sg_transpose_work_bytes(n, m, nblk))
-    work = torch.empty(wb, dtype=torch.uint8, device=dev)
     colptr = torch.empty(m + 1, dtype=torch.int64, device=dev)
     rowidx = torch.empty(max(S.nnz, 1), dtype=torch.int32, device=dev)
-    scan = torch.empty(int(L.sg_scan_scratch_bytes(max(n, m) + 1)), dtype=torch.uint8, device=dev)
-    _lib.check(L.sg_csr_transpose(n, m, S.indptr.data_ptr(), S.indices.data_ptr(), None, nblk, work.data_ptr(), wb,
-                                  colptr.data_ptr(), rowidx.data_ptr(), None, scan.data_ptr(), st.status_ptr, sh),
-               "transpose")
-    st.raise_if_error("stacked transpose")
-    del work, rowidx
+    cval = torch.empty(max(S.nnz, 1), dtype=torch.float32, device=dev) if S.data is not None else None
+    z0 = 0
+    for d, c in enumerate(mats):
+        cp, ri, cv = _eigen.transpose(c, sh)
+        nz = c.nnz
+        c0, c1 = int(coff[d]), int(coff[d + 1])
+        torch.add(cp[:-1], z0, out=colptr[c0:c1])
+        torch.add(ri, int(roff[d]), out=rowidx[z0:z0 + nz])
+        if cval is not None:
+            cval[z0:z0 + nz].copy_(cv if cv is not None else torch.ones(nz, dtype=torch.float32, device=dev))
+        z0 += nz
+        del cp, ri, cv
+    colptr[m] = z0
+    torch.cuda.synchronize(dev)
+    tm["transpose"] = time.perf_counter() - t0 - tm["stack"]
+    # IDF per dataset (its own cell count), then the stacked operator
     roff_t = torch.from_numpy(roff).to(dev)
     coff_t = torch.from_numpy(coff).to(dev)
     mm = torch.empty(2 * D, dtype=torch.int64, device=dev)
     w = torch.empty(m, dtype=torch.float64, device=dev)
     _lib.check(L.sg_bidf(m, colptr.data_ptr(), D, coff_t.data_ptr(), roff_t.data_ptr(), mm.data_ptr(), w.data_ptr(),
                          sh), "sg_bidf")
-    op = _eigen.build_operator(S, w.cpu().numpy())
-    return BatchedOperator(D, roff, coff, op)
+    op = _eigen.build_operator(S, w, csc=(colptr, rowidx[:S.nnz], cval[:S.nnz] if cval is not None else None))
+    torch.cuda.synchronize(dev)
+    tm["operator"] = time.perf_counter() - t0 - tm["stack"] - tm["transpose"]
+    return BatchedOperator(D, roff, coff, op, tm)
 
 
 def _cta_partition(roff: np.ndarray, target: int):
@@ -216,11 +233,15 @@ def eigsh_lm_batched(bop: BatchedOperator, k: int, *, precision: str = "mixed", 
     settled = np.zeros(D, bool)
     Ys = [None] * D
     pool = ThreadPoolExecutor(max_workers=threads)
+    ph = dict(cycles=0.0, ritz=0.0, restart=0.0, refine=0.0)
     while True:
+        tc = time.perf_counter()
         Me = run_cycle(Q, m0)
         n_mv += (Me - m0) // block
         Hh = H.cpu().numpy()
         st.raise_if_error("batched block Lanczos (rank-deficient Krylov block)")
+        tr = time.perf_counter()
+        ph["cycles"] += tr - tc
 
         def ritz(d):
             th, Y = np.linalg.eigh(Hh[d, :Me, :Me])
@@ -232,13 +253,13 @@ def eigsh_lm_batched(bop: BatchedOperator, k: int, *, precision: str = "mixed", 
             need = np.where(th[sel] > 0, tol_vec, tol_val) * anorm
             return th, Y, Rl, order, float(np.max(res[sel] / need))
 
-        out = list(pool.map(ritz, [d for d in range(D)]))
-        for d in range(D):
-            th, Y, Rl, order, worst = out[d]
-            if not conv[d]:
-                Ys[d] = (th, Y, Rl, order)
-                if worst <= 1.0:
-                    conv[d] = True
+        live = [d for d in range(D) if not conv[d]]  # converged datasets keep their last Ritz pairs
+        for d, (th, Y, Rl, order, worst) in zip(live, pool.map(ritz, live)):
+            Ys[d] = (th, Y, Rl, order)
+            if worst <= 1.0:
+                conv[d] = True
+        tq = time.perf_counter()
+        ph["ritz"] += tq - tr
         if conv.all() or restarts >= max_restarts:
             break
         restarts += 1
@@ -269,6 +290,7 @@ def eigsh_lm_batched(bop: BatchedOperator, k: int, *, precision: str = "mixed", 
         chk(L.sg_bmask(n_tot, D, roff_t.data_ptr(), active.data_ptr(), op.row_mask.data_ptr(), sh0), "mask")
         chk(L.sg_bmask(op.m, D, coff_t.data_ptr(), active.data_ptr(), op.col_mask.data_ptr(), sh0), "mask")
         m0 = keep
+        ph["restart"] += time.perf_counter() - tq
     pool.shutdown()
     op.row_mask = op.col_mask = None
     Ybuf = np.zeros((D, Me, k))
@@ -287,11 +309,13 @@ def eigsh_lm_batched(bop: BatchedOperator, k: int, *, precision: str = "mixed", 
     U = torch.empty(n_tot, k, **f64)
     chk(L.sg_bbasis_rotate(code, 1, ncta, cta_ds.data_ptr(), cta_r0.data_ptr(), cta_r1.data_ptr(), Q.data_ptr(), ld,
                            Me, Yt.data_ptr(), k, Me * k, k, U.data_ptr(), k, sh0), "batched rotate")
+    tf = time.perf_counter()
     if refine and precision == "mixed" and k <= 32:
         ev_out, U = _refine_batched(op, D, k, U, ncta, cta_ds, cta_r0, cta_r1, ds_cta, sh0)
     torch.cuda.synchronize(dev)
+    ph["refine"] = time.perf_counter() - tf
     info = dict(block_matvecs=n_mv, restarts=restarts, converged=int(conv.sum()), datasets=D, basis=M, keep=keep,
-                graphs=len(graphs), seconds=time.perf_counter() - t0)
+                graphs=len(graphs), seconds=time.perf_counter() - t0, phase_seconds=ph)
     return BatchedResult(ev_out, U, roff, info)
 
 

@@ -123,7 +123,9 @@ class GramOperator:
             rows, cols = (self.m, self.n) if which == 0 else (self.n, self.m)
             ptr, idx = (self.colptr, self.rowidx) if which == 0 else (self.csr.indptr, self.csr.indices)
             nb = int(L.sg_staged_table_bytes(dtype_code, block, rows, cols))
-            if nb <= 0:
+            # a table larger than half the column indices means segments of a
+            # few nonzeros per (row, stage): the staged schedule cannot pay off
+            if nb <= 0 or nb > 2 * max(int(idx.numel()), 1):
                 raise _lib.SnapGB300Error(_lib.SG_ERR_ARG, "staged SpMM: shape not supported")
             t = torch.empty(nb, dtype=torch.uint8, device=self.a.device)
             _lib.check(L.sg_staged_table(dtype_code, block, rows, cols, ptr.data_ptr(), idx.data_ptr(),
@@ -254,14 +256,13 @@ def select_columns(csr: DeviceCSR, features: np.ndarray | None) -> DeviceCSR:
     return DeviceCSR(optr, oidx[:k], oval[:k] if oval is not None else None, (n, int(feats.shape[0])))
 
 
-def build_operator(csr: DeviceCSR, feature_weights=None) -> GramOperator:
-    """Transpose, IDF weights, row norms and degrees (embedding.rs:42-47,139-152)."""
+def transpose(csr: DeviceCSR, stream: int | None = None):
+    """(colptr, rowidx, cvalues) of X: deterministic CSR -> CSC on the GPU.
+    Raises ValueError on unsorted, duplicate or out-of-range column indices."""
     L = _lib.lib()
     dev = csr.indptr.device
     n, m = csr.shape
-    if n < 2 or m < 1:
-        raise ValueError("need at least 2 cells and 1 feature")
-    sh = torch.cuda.current_stream(dev).cuda_stream
+    sh = torch.cuda.current_stream(dev).cuda_stream if stream is None else stream
     st = _lib.DeviceStatus(dev)
     nblk = int(L.sg_transpose_blocks())
     nblk = max(1, min(nblk, n))
@@ -277,11 +278,28 @@ def build_operator(csr: DeviceCSR, feature_weights=None) -> GramOperator:
                                   cval.data_ptr() if cval is not None else None, scan.data_ptr(),
                                   st.status_ptr, sh), "sg_csr_transpose")
     del work
-    # the set-up kernels below index through X: stop here on invalid indices
+    # the set-up kernels that follow index through X: stop here on invalid indices
     try:
         st.raise_if_error("CSR transpose")
     except _lib.SnapGB300Error as e:
         raise ValueError("X must be CSR with sorted, unique, in-range column indices") from e
+    return colptr, rowidx[:csr.nnz], cval[:csr.nnz] if cval is not None else None
+
+
+def build_operator(csr: DeviceCSR, feature_weights=None, csc=None) -> GramOperator:
+    """Transpose, IDF weights, row norms and degrees (embedding.rs:42-47,139-152).
+
+    ``csc`` = (colptr, rowidx, cvalues) of the same matrix skips the transpose
+    (the batched path assembles it from per-dataset transposes)."""
+    L = _lib.lib()
+    dev = csr.indptr.device
+    n, m = csr.shape
+    if n < 2 or m < 1:
+        raise ValueError("need at least 2 cells and 1 feature")
+    sh = torch.cuda.current_stream(dev).cuda_stream
+    st = _lib.DeviceStatus(dev)
+    colptr, rowidx, cval = transpose(csr, sh) if csc is None else csc
+    vptr = csr.data.data_ptr() if csr.data is not None else None
     f64 = dict(dtype=torch.float64, device=dev)
     f32 = dict(dtype=torch.float32, device=dev)
     w, w2, rinv, colsum = (torch.empty(m, **f64), torch.empty(m, **f64), torch.empty(n, **f64),
@@ -290,8 +308,11 @@ def build_operator(csr: DeviceCSR, feature_weights=None) -> GramOperator:
     w2_32, a32, dinv32 = torch.empty(m, **f32), torch.empty(n, **f32), torch.empty(n, **f32)
     mm = torch.empty(2, dtype=torch.int64, device=dev)
     fw = None
-    if feature_weights is not None:
+    if isinstance(feature_weights, torch.Tensor):
+        fw = feature_weights.to(dev, torch.float64).contiguous()
+    elif feature_weights is not None:
         fw = torch.as_tensor(np.asarray(feature_weights, dtype=np.float64)).to(dev)
+    if fw is not None:
         if fw.shape[0] != m:
             raise ValueError(f"feature_weights has {fw.shape[0]} entries, expected {m}")
     _lib.check(L.sg_spectral_prepare(n, m, csr.indptr.data_ptr(), csr.indices.data_ptr(), vptr,
@@ -310,8 +331,7 @@ def build_operator(csr: DeviceCSR, feature_weights=None) -> GramOperator:
             raise ValueError(f"cell {e.bad_index} has no selected features or shares none with any other "
                              "cell; the cosine operator is undefined (the reference produces NaN)") from e
         raise
-    return GramOperator(n, m, csr, colptr, rowidx[:csr.nnz], cval[:csr.nnz] if cval is not None else None,
-                        w, w2, a, dinv, w2_32, a32, dinv32, rinv)
+    return GramOperator(n, m, csr, colptr, rowidx, cval, w, w2, a, dinv, w2_32, a32, dinv32, rinv)
 
 
 @dataclass
@@ -395,7 +415,9 @@ def eigsh_lm(op: GramOperator, k: int, *, precision: str = "mixed", block: int =
     n_mv = 0
     restarts = 0
     hist = []
+    ph = dict(cycles=0.0, ritz=0.0, restart=0.0, refine=0.0)
     while True:
+        tc = time.perf_counter()
         while m + block <= M:
             op.apply(code, block, Z, Zs, T, W, sh)
             n_mv += 1
@@ -416,6 +438,8 @@ def eigsh_lm(op: GramOperator, k: int, *, precision: str = "mixed", block: int =
         Me = m
         Hh = H.cpu().numpy()
         st.raise_if_error("block Lanczos (rank-deficient Krylov block)")
+        tr = time.perf_counter()
+        ph["cycles"] += tr - tc
         th, Y = np.linalg.eigh(Hh[:Me, :Me])
         Rl = Hh[Me:Me + block, Me - block:Me]
         res = np.linalg.norm(Rl @ Y[Me - block:Me, :], axis=0)
@@ -425,6 +449,8 @@ def eigsh_lm(op: GramOperator, k: int, *, precision: str = "mixed", block: int =
         need = np.where((th[sel] > 0) | (not vec_positive_only), tol_vec, tol_val) * anorm
         worst = float(np.max(res[sel] / need))
         hist.append(float(res[sel].max()))
+        tq = time.perf_counter()
+        ph["ritz"] += tq - tr
         if worst <= 1.0 or restarts >= max_restarts:
             break
         if precision == "mixed" and len(hist) >= 6 and min(hist[-3:]) > 0.7 * min(hist[:-3]):
@@ -444,6 +470,7 @@ def eigsh_lm(op: GramOperator, k: int, *, precision: str = "mixed", block: int =
         Hn[:keep, keep:keep + block] = Bc.T
         H.copy_(torch.from_numpy(Hn))
         m = keep
+        ph["restart"] += time.perf_counter() - tq
     # Ritz vectors (FP64 output), eigenvalues sorted descending like the reference
     sel = order[:k]
     sel = sel[np.argsort(-th[sel], kind="stable")]
@@ -452,13 +479,15 @@ def eigsh_lm(op: GramOperator, k: int, *, precision: str = "mixed", block: int =
     _lib.check(L.sg_basis_rotate(code, 1, n, Q.data_ptr(), ld, Me, Yk.data_ptr(), k, k, U.data_ptr(), k, sh),
                "rotate")
     evals = th[sel].copy()
+    tf = time.perf_counter()
     if refine and precision == "mixed" and k <= 32:
         evals, U = fp64_refine(op, U, k, sh)
     torch.cuda.synchronize(dev)
+    ph["refine"] = time.perf_counter() - tf
     beyond = order[k:k + 4]  # Ritz values just outside the wanted set
     info = dict(block_matvecs=n_mv, vector_matvecs=n_mv * block, restarts=restarts, basis=M, keep=keep,
                 residuals=res[sel].tolist(), converged=worst <= 1.0, seconds=time.perf_counter() - t0,
-                precision=precision, block=block, next_evals=th[beyond].tolist())
+                precision=precision, block=block, next_evals=th[beyond].tolist(), phase_seconds=ph)
     return EigenResult(evals, U, info)
 
 
