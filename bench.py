@@ -325,6 +325,10 @@ def run_gpu(args):
         xb += c
     n_launch = 2 * len(spmm_ev)
     spmm_ms = (t_time + x_time) / max(n_launch, 1)
+    # DRAM traffic per launch: ncu dram__bytes_read.sum + dram__bytes_write.sum of both passes at
+    # 20,000 cells x 500,000 features came to 0.997 (Xᵀ pass) and 1.005 (X pass) of the algorithmic
+    # bytes; both grow with nnz, so the 100k launch is scaled from its own algorithmic bytes
+    traffic = (0.997 * tb + 1.005 * xb) / max(n_launch, 1)
     achieved = (tb + xb) / max((t_time + x_time) / 1e3, 1e-12) / 1e9
     peak, peak_kind = peaks()
     spmm_share = (t_time + x_time) / (ms * args.steps)
@@ -411,7 +415,8 @@ def run_gpu(args):
         "roofline": {"kernel": "spmm_kernel (Gram matvec, Xᵀ gather over CSC + X gather over CSR)",
                      "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_kind,
-                     "traffic": None, "launches": n_launch, "avg_launch_ms": spmm_ms,
+                     "traffic": traffic, "traffic_unit": "bytes per launch (ncu at 20k cells, scaled by nnz)",
+                     "launches": n_launch, "avg_launch_ms": spmm_ms,
                      "bytes_per_block_matvec": int((tb + xb) / max(len(spmm_ev), 1)),
                      "share_of_step": spmm_share},
         "gpu_launches": launches,

@@ -104,6 +104,22 @@ int sg_tile_emit(int64_t n_cells, const int64_t* key_ptr, const void* scratch,
 
 
 /* ------------------------------------------------------------------------ */
+/* Feature selection -- the `count` vector of select_features              */
+/*   (snapatac2-python/python/snapatac2/preprocessing/_basic.py:1053-1056:   */
+/*   FP64 column sums of X).  The ranking itself (_basic.py:952-967, NumPy  */
+/*   argsort tie order) stays with the caller.                               */
+/* ------------------------------------------------------------------------ */
+
+/* out[m] = column sums of the CSR entries.  counts (uint32) or values      */
+/* (float32) or neither (binary pattern: 1 per entry), not both.  Integer   */
+/* inputs are summed exactly in uint64 (scratch: m uint64) and converted:    */
+/* identical to the reference's FP64 sums.  Float values are summed in FP64  */
+/* (scratch unused).  Out-of-range column indices set status SG_ERR_ARG      */
+/* with the first offending entry in bad.                                    */
+int sg_col_counts(int64_t nnz, int64_t m, const int32_t* indices, const uint32_t* counts, const float* values,
+                  double* out, unsigned long long* scratch, int* status, unsigned long long* bad, void* stream);
+
+/* ------------------------------------------------------------------------ */
 /* Spectral embedding (matrix-free cosine) -- replaces spectral_embedding    */
 /*   (snapatac2-python/src/embedding.rs:24-59): column slice + idf +         */
 /*   normalize + spectral_mf degree (embedding.rs:133-152,269-286,315-326)   */

@@ -24,6 +24,7 @@ import numpy as np
 import torch
 
 from . import _eigen, _lib
+from ._hostblas import blas_threads
 from ._binning import DeviceCSR
 
 _DT = {"mixed": (0, torch.float32), "fp64": (1, torch.float64)}
@@ -254,7 +255,9 @@ def eigsh_lm_batched(bop: BatchedOperator, k: int, *, precision: str = "mixed", 
             return th, Y, Rl, order, float(np.max(res[sel] / need))
 
         live = [d for d in range(D) if not conv[d]]  # converged datasets keep their last Ritz pairs
-        for d, (th, Y, Rl, order, worst) in zip(live, pool.map(ritz, live)):
+        with blas_threads(1):  # one LAPACK thread per pool thread
+            out = list(pool.map(ritz, live))
+        for d, (th, Y, Rl, order, worst) in zip(live, out):
             Ys[d] = (th, Y, Rl, order)
             if worst <= 1.0:
                 conv[d] = True

@@ -41,6 +41,7 @@ SIGNATURES: dict[str, tuple] = {
     "sg_tile_run": (_I32, [_P, _I64, _I64, _P, _P, _P, _P, _P, _I32, _U32, _I32, _I64, _I64, _P, _P,
                            _I64, _P, _P, _P, _P, _P]),
     "sg_tile_emit": (_I32, [_I64, _P, _P, _I64, _P, _P, _P, _I64, _P, _P]),
+    "sg_col_counts": (_I32, [_I64, _I64, _P, _P, _P, _P, _P, _P, _P, _P]),
     "sg_csr_select_cols": (_I32, [_I64, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
     "sg_transpose_blocks": (_I32, []),
     "sg_transpose_work_bytes": (_I64, [_I64, _I64, _I32]),
@@ -85,7 +86,7 @@ SIGNATURES: dict[str, tuple] = {
 # benchmark): e.g. sg_block_cholqr = projection partial + reduce + Cholesky +
 # R⁻¹ application.
 KERNELS_PER_CALL = {
-    "sg_tile_plan": 4, "sg_tile_run": 5, "sg_tile_emit": 1, "sg_csr_select_cols": 5,
+    "sg_tile_plan": 4, "sg_tile_run": 5, "sg_tile_emit": 1, "sg_col_counts": 2, "sg_csr_select_cols": 5,
     "sg_csr_transpose": 8, "sg_spectral_prepare": 7, "sg_spmm": 1, "sg_spmm_ex": 1, "sg_spmm_masked": 1,
     "sg_spmm_staged": 1, "sg_staged_table": 1, "sg_block_proj": 2, "sg_block_update": 1, "sg_block_cholqr": 4, "sg_block_finish": 1,
     "sg_lanczos_hblock": 1, "sg_basis_rotate": 1, "sg_fill_random": 1, "sg_knn": 6, "sg_knn_noalloc": 6,

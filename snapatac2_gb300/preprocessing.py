@@ -159,29 +159,74 @@ def _find_most_accessible_features(feature_count, filter_lower_quantile, filter_
     return order[::-1][:total_features]
 
 
+def column_counts(X, device=None) -> np.ndarray:
+    """FP64 column sums of a cell-by-feature matrix on the GPU (sg_col_counts),
+    the ``count`` of ``_basic.py:1053-1056``.  ``X`` is a SciPy sparse matrix
+    or a DeviceCSR; integer counts are summed exactly, so the result equals
+    the reference's FP64 sums bit for bit."""
+    from . import _lib
+    from ._binning import DeviceCSR
+    L = _lib.lib()
+    dev = _device(device)
+    if isinstance(X, DeviceCSR):
+        n, m = X.shape
+        idx = X.indices.to(dev)
+        vals = None if X.data is None else X.data.to(dev)
+    else:
+        X = sp.csr_matrix(X)
+        n, m = X.shape
+        idx = torch.from_numpy(np.ascontiguousarray(X.indices, dtype=np.int32)).to(dev)
+        d = X.data
+        integral = d.size == 0 or (d.min() >= 0 and d.max() <= 0xFFFFFFFF and
+                                   (d.dtype.kind in "ui" or bool(np.all(d == np.floor(d)))))
+        if integral:  # uint32 count bits in an int32 tensor
+            vals = torch.from_numpy(np.ascontiguousarray(d.astype(np.uint32)).view(np.int32)).to(dev)
+        else:
+            vals = torch.from_numpy(np.ascontiguousarray(d, dtype=np.float32)).to(dev)
+    if m == 0:
+        return np.zeros(0)
+    out = torch.empty(m, dtype=torch.float64, device=dev)
+    scratch = torch.empty(m, dtype=torch.int64, device=dev)
+    st = _lib.DeviceStatus(dev)
+    cnt_ptr = val_ptr = None
+    if vals is not None:
+        if vals.dtype == torch.int32:
+            cnt_ptr = vals.data_ptr()
+        else:
+            vals = vals.to(torch.float32)
+            val_ptr = vals.data_ptr()
+    sh = torch.cuda.current_stream(dev).cuda_stream
+    _lib.check(L.sg_col_counts(int(idx.numel()), m, idx.data_ptr() if idx.numel() else None, cnt_ptr, val_ptr,
+                               out.data_ptr(), scratch.data_ptr(), st.status_ptr, st.bad_ptr, sh), "sg_col_counts")
+    st.raise_if_error("column counts (column index out of range)")
+    return out.cpu().numpy()
+
+
 def select_features(adata, n_features: int = 500000, filter_lower_quantile: float = 0.005,
                     filter_upper_quantile: float = 0.005, whitelist=None, blacklist=None,
-                    max_iter: int = 1, inplace: bool = True, n_jobs: int = 8, verbose: bool = True):
-    """Most-accessible-feature selection (``_basic.py:969-1095``), host NumPy.
+                    max_iter: int = 1, inplace: bool = True, n_jobs: int = 8, verbose: bool = True, *,
+                    device=None):
+    """Most-accessible-feature selection (``_basic.py:969-1095``).
 
-    The mask depends on NumPy's unstable argsort tie order, so it is computed
-    once on the host and shared by every consumer.  Sets ``var['count']`` and
-    ``var['selected']`` in place, or returns the boolean mask.
+    The column counts are summed on the GPU (``column_counts``); the ranking
+    depends on NumPy's unstable argsort tie order, so it runs on the host as
+    in the reference and its mask is shared by every consumer.  Sets
+    ``var['count']`` and ``var['selected']`` in place, or returns the mask.
     """
     if isinstance(adata, list):
         res = [select_features(a, n_features, filter_lower_quantile, filter_upper_quantile, whitelist,
-                               blacklist, max_iter, inplace, verbose=False) for a in adata]
+                               blacklist, max_iter, inplace, verbose=False, device=device) for a in adata]
         return None if inplace else res
     if whitelist is not None or blacklist is not None:
         raise NotImplementedError("whitelist/blacklist BED filtering is not supported")
     if max_iter != 1:
         raise NotImplementedError("iterative feature selection (max_iter > 1) is not supported")
-    X = sp.csr_matrix(adata.X)
-    count = np.bincount(X.indices, weights=X.data.astype(np.float64), minlength=X.shape[1])
+    X = adata.X
+    count = column_counts(X, device)
     if inplace:
         adata.var["count"] = count
     sel = _find_most_accessible_features(count, filter_lower_quantile, filter_upper_quantile, n_features)
-    result = np.zeros(X.shape[1], dtype=bool)
+    result = np.zeros(count.shape[0], dtype=bool)
     result[sel] = True
     if verbose:
         logging.info(f"Selected {result.sum()} features.")
