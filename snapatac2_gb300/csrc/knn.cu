@@ -6,14 +6,18 @@
 // Pipeline (no host synchronisation):
 //  1. prep    X (n x d FP64) -> zero-padded FP32 and FP64 copies (n x DP),
 //             max row norm.
-//  2. scan    tiled brute force in FP32: a CTA owns 32 queries (one per lane,
-//             query vector in registers) and streams 128-candidate tiles
-//             through shared memory; each warp computes 32 x 16 distances
-//             with broadcast float4 loads, then a fused warp-level top-K'
-//             selection (K' = k + margin) keeps per-query candidate lists in
-//             shared memory: candidates below the current K'-th distance are
-//             appended by ballot and the list is re-sorted (warp bitonic)
-//             when it overflows.
+//  2. scan    tiled brute force in FP32, filter then verify: a CTA owns 32
+//             queries and streams 128-candidate tiles (stored tile-transposed,
+//             so a tile is one coalesced 16 KB copy) through shared memory.
+//             Filter: every thread computes 4 queries x 4 candidates in the
+//             expanded form |q|^2 + |c|^2 - 2 q.c (one FFMA per dimension and
+//             pair) and keeps the pairs that pass the current K'-th distance
+//             tau widened by a bound on the FP32 error of that form (so no
+//             pair whose exact-order difference-form distance is below tau is
+//             dropped).  Verify: the warp recomputes the kept pairs in the
+//             difference form sum (q_t - c_t)^2 (the FP32 arithmetic the
+//             certificate below is stated for) and appends those below tau to
+//             the query's list, re-sorted (warp bitonic) when it overflows.
 //  3. rerank  FP64 distances of the K' candidates, sort by (distance, index),
 //             keep k.  Certificate: every point outside the list has FP32
 //             distance >= tau (the K'-th), hence FP64 distance >= tau - delta
@@ -67,7 +71,6 @@ __device__ void warp_bitonic(K* key, int* idx, int N) {
 }
 
 template <typename K> __device__ __forceinline__ K kinf();
-template <> __device__ __forceinline__ float kinf<float>() { return FLT_MAX; }
 template <> __device__ __forceinline__ double kinf<double>() { return DBL_MAX; }
 
 template <typename TD, int DP>
@@ -210,6 +213,234 @@ scan_kernel(const TD* __restrict__ Xp, int64_t n, const int* __restrict__ qlist,
   }
 }
 
+// ---------------------------------------------------------------------------
+// FP32 filter-verify scan (step 2).  XT holds the centred FP32 points tile-
+// transposed: tile t (points 128t .. 128t+127) at XT + t*DP*128, coordinate
+// (dim, j) at [dim*128 + j], zero beyond n; nrm[i] = FP32 of |x_i - mean|^2.
+// ---------------------------------------------------------------------------
+constexpr int kFQ = 32;          // queries per CTA
+constexpr int kFC = 128;         // candidates per tile
+constexpr int kFW = 8;           // warps per CTA (warp w owns queries 4w .. 4w+3)
+constexpr int kFBuf = 3;         // candidate tiles in flight (ring)
+
+// LIST entries per query: the kept Kp plus one verify batch of 32 (a list is
+// re-sorted before a batch that would not fit), so LIST >= Kp + 32.
+template <int DP, int LIST>
+struct FilterSmem {
+  uint64_t full[kFBuf];                      // tile k landed in buffer k % kFBuf
+  uint64_t empty[kFBuf];                     // every warp is done with that buffer
+  __align__(16) float cT[kFBuf][DP][kFC];    // candidate tiles (bulk copies of XT)
+  __align__(16) float cn[kFBuf][kFC];        // their squared norms (bulk copies of nrm)
+  __align__(16) float qT[DP][kFQ];
+  float lk[kFQ][LIST];
+  int li[kFQ][LIST];
+  int cnt[kFQ];
+  float tau[kFQ];
+  unsigned queue[kFW][kFC];                  // one query's filtered candidates of a tile
+  int nqueue[kFW];
+};
+
+// Sort one query's list (warp), keep Kp, update its tau.
+template <int LIST>
+__device__ void merge_list_f(float* lk, int* li, int* cnt, float* tau, int Kp) {
+  const int lane = threadIdx.x & 31;
+  const int c = *cnt;
+  for (int t = c + lane; t < LIST; t += 32) {
+    lk[t] = FLT_MAX;
+    li[t] = 0x7fffffff;
+  }
+  __syncwarp();
+  warp_bitonic<float>(lk, li, LIST);
+  __syncwarp();
+  if (lane == 0) {
+    const int keep = c < Kp ? c : Kp;
+    *cnt = keep;
+    *tau = keep == Kp ? lk[Kp - 1] : FLT_MAX;
+  }
+  __syncwarp();
+}
+
+// Warps advance through the tiles on their own: a tile is consumed once its
+// copy lands (full barrier), and its buffer is refilled only after all
+// warps arrived on its empty barrier, so a warp busy re-sorting a list holds
+// up the others only once they run a whole ring ahead.  Thread 0 produces.
+template <int DP, int LIST>
+__global__ void __launch_bounds__(kFW * 32, 2)
+filter_scan_kernel(const float* __restrict__ XT, const float* __restrict__ nrm, int64_t n, int d, int Kp,
+                   int* __restrict__ cand, float* __restrict__ tau_out) {
+  extern __shared__ __align__(16) unsigned char sraw[];
+  FilterSmem<DP, LIST>& sm = *reinterpret_cast<FilterSmem<DP, LIST>*>(sraw);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int64_t qbase = (int64_t)blockIdx.x * kFQ;
+  const int64_t ntiles = (n + kFC - 1) / kFC;
+  constexpr uint32_t kTileBytes = DP * kFC * 4, kNormBytes = kFC * 4;
+  auto issue = [&](int64_t k) {
+    const int b = (int)(k % kFBuf);
+    mbar_expect_tx(&sm.full[b], kTileBytes + kNormBytes);
+    bulk_copy(&sm.cT[b][0][0], XT + k * DP * kFC, kTileBytes, &sm.full[b]);
+    bulk_copy(&sm.cn[b][0], nrm + k * kFC, kNormBytes, &sm.full[b]);
+  };
+  if (threadIdx.x == 0) {
+    for (int b = 0; b < kFBuf; ++b) {
+      mbar_init(&sm.full[b], 1);
+      mbar_init(&sm.empty[b], kFW);
+    }
+    fence_barrier_init();
+    fence_proxy_async();
+    for (int64_t k = 0; k < kFBuf - 1 && k < ntiles; ++k) issue(k);
+  }
+  {
+    const float* src = XT + (qbase / kFC) * DP * kFC + (qbase % kFC);
+    for (int e = threadIdx.x; e < DP * kFQ; e += blockDim.x) sm.qT[e / kFQ][e % kFQ] = src[(e / kFQ) * kFC + e % kFQ];
+  }
+  if (threadIdx.x < kFQ) {
+    sm.cnt[threadIdx.x] = 0;
+    sm.tau[threadIdx.x] = FLT_MAX;
+  }
+  if (lane == 0) sm.nqueue[wid] = 0;
+  float qn[4];
+  int64_t qid[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    qid[i] = qbase + 4 * wid + i;
+    qn[i] = qid[i] < n ? nrm[qid[i]] : 0.f;
+  }
+  __syncthreads();
+  // Filter bound.  With u = 2^-24, s the FP32 dot product (FMA chain over DP
+  // terms), nq, nc the FP32 squared norms and D^ the exact squared distance
+  // of the FP32 points: |(nq + nc - 2 s) - D^| <= (DP + 3) u (nq + nc) + u D^,
+  // and the difference-form FP32 distance d32 obeys |d32 - D^| <= (d + 3) u D^.
+  // So d32 < tau implies nq + nc - 2 s < tau + Ku (nq + nc) + Tu tau with
+  // K = 2 DP + 16, T = 4 (d + 4) (twice the derived constants, which also
+  // covers the rounding of the test itself), written as
+  // nc (1 - Ku) - 2 s < tau (1 + Tu) + Ku nq - nq.
+  const float u = 5.9604644775390625e-08f;
+  const float Ku = (float)(2 * DP + 16) * u, Tu = (float)(4 * (d + 4)) * u;
+  const float kInf = __int_as_float(0x7f800000);
+  bool failed = false;
+  int64_t issued = kFBuf - 1 < ntiles ? kFBuf - 1 : ntiles;  // tiles handed to the copy engine (thread 0)
+  for (int64_t k = 0; k < ntiles; ++k) {
+    const int b = (int)(k % kFBuf);
+    bool pfail = false;
+    if (threadIdx.x == 0 && k + kFBuf - 1 < ntiles) {
+      // refill the buffer tile k - 1 used, once every warp is done with it
+      const int64_t kn = k + kFBuf - 1;
+      const bool ok = kn < kFBuf || mbar_wait(&sm.empty[kn % kFBuf], (uint32_t)(((kn / kFBuf) - 1) & 1));
+      if (ok) {
+        fence_proxy_async();
+        issue(kn);
+        issued = kn + 1;
+      } else {
+        pfail = true;
+      }
+    }
+    const bool got = !pfail && mbar_wait(&sm.full[b], (uint32_t)((k / kFBuf) & 1));
+    if (!__all_sync(0xffffffffu, got)) {
+      failed = true;  // a tile never landed: leave this warp's queries to the exact rescan
+      break;
+    }
+    const int64_t c0 = k * kFC;
+    float T[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const float tq = sm.tau[4 * wid + i];
+      T[i] = qid[i] >= n ? -kInf : (tq >= FLT_MAX ? kInf : (tq + Tu * tq) + (Ku * qn[i] - qn[i]));
+    }
+    float acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
+#pragma unroll 8
+    for (int t = 0; t < DP; ++t) {
+      const float4 qv = *reinterpret_cast<const float4*>(&sm.qT[t][4 * wid]);
+      const float4 cv = *reinterpret_cast<const float4*>(&sm.cT[b][t][4 * lane]);
+      const float qa[4] = {qv.x, qv.y, qv.z, qv.w}, ca[4] = {cv.x, cv.y, cv.z, cv.w};
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(qa[i], ca[j], acc[i][j]);
+    }
+    const float4 cn4 = *reinterpret_cast<const float4*>(&sm.cn[b][4 * lane]);
+    const float cadj[4] = {cn4.x * (1.0f - Ku), cn4.y * (1.0f - Ku), cn4.z * (1.0f - Ku), cn4.w * (1.0f - Ku)};
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int q = 4 * wid + i;
+      const int64_t so = qid[i] - c0;  // the query's own column in this tile, if any
+      const int self = (so >= 0 && so < kFC) ? (int)so : -1;
+      bool keep[4];
+      bool any = false;
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        keep[j] = fmaf(-2.0f, acc[i][j], cadj[j]) < T[i] && 4 * lane + j != self;
+        any |= keep[j];
+      }
+      if (!__any_sync(0xffffffffu, any)) continue;  // nothing of this query passed the filter
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+        if (keep[j]) sm.queue[wid][atomicAdd(&sm.nqueue[wid], 1)] = (unsigned)(4 * lane + j);
+      __syncwarp();
+      // verify in the difference form; append (ballot order) those below tau,
+      // re-sorting the list first when the batch would not fit
+      const int nk = sm.nqueue[wid];
+      int cq = sm.cnt[q];
+      for (int e0 = 0; e0 < nk; e0 += 32) {
+        const int e = e0 + lane;
+        int c = 0;
+        float dd = kInf;
+        if (e < nk) {
+          c = (int)sm.queue[wid][e];
+          dd = 0.f;
+#pragma unroll
+          for (int t = 0; t < DP; ++t) {
+            const float df = sm.qT[t][q] - sm.cT[b][t][c];
+            dd = fmaf(df, df, dd);
+          }
+        }
+        bool pass = dd < sm.tau[q];
+        unsigned bal = __ballot_sync(0xffffffffu, pass);
+        if (cq + __popc(bal) > LIST) {
+          if (lane == 0) sm.cnt[q] = cq;
+          __syncwarp();
+          merge_list_f<LIST>(sm.lk[q], sm.li[q], &sm.cnt[q], &sm.tau[q], Kp);
+          cq = sm.cnt[q];
+          pass = dd < sm.tau[q];
+          bal = __ballot_sync(0xffffffffu, pass);
+        }
+        if (pass) {
+          const int p = cq + __popc(bal & lanemask_lt());
+          sm.lk[q][p] = dd;
+          sm.li[q][p] = (int)(c0 + c);
+        }
+        cq += __popc(bal);
+      }
+      if (lane == 0) {
+        sm.cnt[q] = cq;
+        sm.nqueue[wid] = 0;
+      }
+      __syncwarp();
+    }
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&sm.empty[b]);  // this warp is done with buffer b
+  }
+  failed = __any_sync(0xffffffffu, failed);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int q = 4 * wid + i;
+    if (!failed) merge_list_f<LIST>(sm.lk[q], sm.li[q], &sm.cnt[q], &sm.tau[q], Kp);
+    if (qid[i] < n) {
+      const int c = failed ? 0 : sm.cnt[q];
+      for (int t = lane; t < Kp; t += 32) cand[qid[i] * Kp + t] = t < c ? sm.li[q][t] : -1;
+      if (lane == 0) tau_out[qid[i]] = failed ? -1.0f : sm.tau[q];  // negative tau: certificate fails
+    }
+  }
+  // no copy may still be landing in this CTA's shared memory when it exits:
+  // after a failure, wait (bounded) for the last tiles thread 0 issued
+  if (threadIdx.x == 0 && failed)
+    for (int64_t t = issued - kFBuf < 0 ? 0 : issued - kFBuf; t < issued; ++t)
+      mbar_wait(&sm.full[t % kFBuf], (uint32_t)((t / kFBuf) & 1));
+}
+
 constexpr int kMeanParts = 256;
 
 // Column means of X (n x d FP64), deterministic: per-CTA partial sums, then a
@@ -234,23 +465,35 @@ __global__ void mean_reduce(const double* __restrict__ part, int nparts, int64_t
   mean[t] = t < d ? s / (double)n : 0.0;
 }
 
-// X -> centred, padded FP32 copy and padded FP64 copy (uncentred: the re-rank
-// uses the reference's arithmetic on the original coordinates); max centred
-// row norm (as float bits, rounded up).
+// X -> centred FP32 copy, tile-transposed for the filter scan (XT, zero
+// beyond n up to the tile boundary), its FP32 squared norms, the padded FP64
+// copy (uncentred: the re-rank uses the reference's arithmetic on the
+// original coordinates) and the max centred row norm (float bits, rounded up).
 template <int DP>
 __global__ void prep_kernel(const double* __restrict__ X, int64_t n, int d, const double* __restrict__ mean,
-                            float* __restrict__ X32, double* __restrict__ X64, unsigned* __restrict__ maxnorm_bits) {
+                            float* __restrict__ XT, float* __restrict__ nrm, double* __restrict__ X64,
+                            unsigned* __restrict__ maxnorm_bits) {
   float mx = 0.f;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    double s = 0.0;
+  const int64_t npad = (n + kFC - 1) / kFC * kFC;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < npad; i += (int64_t)gridDim.x * blockDim.x) {
+    float* dst = XT + (i / kFC) * DP * kFC + (i % kFC);
+    if (i >= n) {
+      for (int t = 0; t < DP; ++t) dst[t * kFC] = 0.f;
+      nrm[i] = __int_as_float(0x7f800000);  // never passes the filter
+      continue;
+    }
+    double s = 0.0, s32 = 0.0;
 #pragma unroll 4
     for (int t = 0; t < DP; ++t) {
       const double v = t < d ? X[i * d + t] : 0.0;
       const double c = t < d ? v - mean[t] : 0.0;
-      X32[i * DP + t] = (float)c;
+      const float c32 = (float)c;
+      dst[t * kFC] = c32;
       X64[i * DP + t] = v;
       s += c * c;
+      s32 += (double)c32 * (double)c32;
     }
+    nrm[i] = (float)s32;
     mx = fmaxf(mx, (float)sqrt(s) * 1.0000002f);
   }
   for (int o = 16; o; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
@@ -367,7 +610,8 @@ __global__ void zero_int(int* p, unsigned* u) {
 struct KnnScratch {
   double* mpart;
   double* mean;
-  float* X32;
+  float* XT;
+  float* nrm;
   double* X64;
   int* cand;
   float* tau32;
@@ -385,14 +629,17 @@ KnnScratch knn_layout(char* base, int64_t n, int DP, int k, int Kp) {
   KnnScratch s{};
   int64_t o = 0;
   auto take = [&](int64_t b) { int64_t r = o; o += align256(b); return r; };
+  const int64_t npad = (n + kFC - 1) / kFC * kFC;
   const int64_t omp = take((int64_t)kMeanParts * 64 * 8), omean = take(64 * 8);
-  const int64_t oX32 = take(n * DP * 4), oX64 = take(n * DP * 8), oc = take(n * (int64_t)Kp * 4),
+  const int64_t oXT = take(npad * DP * 4), onrm = take(npad * 4), oX64 = take(n * DP * 8),
+                oc = take(n * (int64_t)Kp * 4),
                 ot = take(n * 4), of = take(n * 4), ofc = take(n * (int64_t)k * 4),
                 ofd = take(n * (int64_t)k * 8), on = take(16);
   if (base) {
     s.mpart = (double*)(base + omp);
     s.mean = (double*)(base + omean);
-    s.X32 = (float*)(base + oX32);
+    s.XT = (float*)(base + oXT);
+    s.nrm = (float*)(base + onrm);
     s.X64 = (double*)(base + oX64);
     s.cand = (int*)(base + oc);
     s.tau32 = (float*)(base + ot);
@@ -420,15 +667,34 @@ int launch_scan(const TD* Xp, int64_t n, const int* qlist, const int* qcount, in
   return cudaGetLastError() == cudaSuccess ? SG_OK : SG_ERR_CUDA;
 }
 
+template <int DP, int LIST>
+int launch_filter_scan_l(const float* XT, const float* nrm, int64_t n, int d, int Kp, int* cand, float* tau,
+                         cudaStream_t s) {
+  const size_t smem = sizeof(FilterSmem<DP, LIST>);
+  if (cudaFuncSetAttribute(filter_scan_kernel<DP, LIST>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+      cudaSuccess)
+    return SG_ERR_CUDA;
+  const int64_t grid = (n + kFQ - 1) / kFQ;
+  filter_scan_kernel<DP, LIST><<<(unsigned)grid, kFW * 32, smem, s>>>(XT, nrm, n, d, Kp, cand, tau);
+  return cudaGetLastError() == cudaSuccess ? SG_OK : SG_ERR_CUDA;
+}
+
+template <int DP>
+int launch_filter_scan(const float* XT, const float* nrm, int64_t n, int d, int Kp, int* cand, float* tau,
+                       cudaStream_t s) {
+  if (Kp + 32 <= 128) return launch_filter_scan_l<DP, 128>(XT, nrm, n, d, Kp, cand, tau, s);
+  return launch_filter_scan_l<DP, 256>(XT, nrm, n, d, Kp, cand, tau, s);
+}
+
 template <int DP>
 int knn_run(const double* X, int64_t n, int d, int k, int Kp, const KnnScratch& w, int64_t* nbr, double* dist,
             cudaStream_t s) {
   zero_int<<<1, 1, 0, s>>>(w.nflag, w.maxnorm);
   mean_partial<<<kMeanParts, 64, 0, s>>>(X, n, d, w.mpart);
   mean_reduce<<<1, 64, 0, s>>>(w.mpart, kMeanParts, n, d, w.mean);
-  prep_kernel<DP><<<grid_for(n, 256, 4096), 256, 0, s>>>(X, n, d, w.mean, w.X32, w.X64, w.maxnorm);
+  prep_kernel<DP><<<grid_for(n, 256, 4096), 256, 0, s>>>(X, n, d, w.mean, w.XT, w.nrm, w.X64, w.maxnorm);
   SG_CHECK_LAUNCH();
-  int e = launch_scan<float, DP>(w.X32, n, nullptr, nullptr, Kp, w.cand, nullptr, w.tau32, s);
+  int e = launch_filter_scan<DP>(w.XT, w.nrm, n, d, Kp, w.cand, w.tau32, s);
   if (e) return e;
   rerank_kernel<DP><<<(unsigned)((n + 7) / 8), 256, 0, s>>>(w.X64, n, d, w.mean, w.cand, Kp, w.tau32, k,
                                                             w.maxnorm, nbr, dist, w.flagged, w.nflag);
@@ -495,11 +761,14 @@ constexpr int64_t kNoAllocMaxN = 16384;  // points
 constexpr int kNoAllocMaxDim = 32;       // dimensions
 constexpr int kNoAllocMaxK = 100;        // neighbours
 constexpr int64_t kA256(int64_t x) { return (x + 255) / 256 * 256; }
-// knn_layout(kNoAllocMaxN, 32, kNoAllocMaxK, kMaxKp) written out: mean partials,
-// mean, X32, X64, candidates, tau, flagged, fallback candidates and
-// distances, counters
+// knn_layout(kNoAllocMaxN, 32, kNoAllocMaxK, kMaxKp) written out (kNoAllocMaxN is
+// a multiple of the 128-point tile): mean partials, mean, tile-transposed
+// FP32 points, their norms, X64, candidates, tau, flagged, fallback
+// candidates and distances, counters
+static_assert(kNoAllocMaxN % kFC == 0, "no-alloc capacity must be whole tiles");
 constexpr int64_t kNoAllocBytes =
-    kA256((int64_t)kMeanParts * 64 * 8) + kA256(64 * 8) + kA256(kNoAllocMaxN * kNoAllocMaxDim * 4) + kA256(kNoAllocMaxN * kNoAllocMaxDim * 8) +
+    kA256((int64_t)kMeanParts * 64 * 8) + kA256(64 * 8) + kA256(kNoAllocMaxN * kNoAllocMaxDim * 4) +
+    kA256(kNoAllocMaxN * 4) + kA256(kNoAllocMaxN * kNoAllocMaxDim * 8) +
     kA256(kNoAllocMaxN * kMaxKp * 4) + kA256(kNoAllocMaxN * 4) + kA256(kNoAllocMaxN * 4) +
     kA256(kNoAllocMaxN * kNoAllocMaxK * 4) + kA256(kNoAllocMaxN * kNoAllocMaxK * 8) + kA256(16);
 

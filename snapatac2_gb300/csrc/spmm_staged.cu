@@ -44,56 +44,6 @@ constexpr int kStagedVariants = 4;
 constexpr int64_t kMaxRowsPerCta = 4096;
 constexpr int kAccSmemBytes = 64 * 1024;
 constexpr int kHeader = 128;               // two mbarriers, padded
-constexpr uint64_t kWaitNs = 2000000000ull;  // bounded stage wait: 2 s
-
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void fence_barrier_init() {
-  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-}
-
-// Orders this thread's earlier generic-proxy shared-memory accesses (and the
-// block's, after a __syncthreads) before later async-proxy ones.
-__device__ __forceinline__ void fence_proxy_async() {
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-}
-
-// One bulk copy of `bytes` (multiple of 16, both addresses 16-byte aligned)
-// global -> shared, completing its bytes on `bar` (armed by the caller).
-__device__ __forceinline__ void bulk_copy(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
-  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                   smem_u32(dst)),
-               "l"(src), "r"(bytes), "r"(smem_u32(bar))
-               : "memory");
-}
-
-__device__ __forceinline__ uint64_t global_ns() {
-  uint64_t t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
-
-// Wait for the phase with this parity to complete; gives up (false) after
-// kWaitNs of wall time, so a copy that never lands cannot hang the kernel.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-  const uint64_t t0 = global_ns();
-  while (true) {
-    uint32_t done;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(done)
-        : "r"(smem_u32(bar)), "r"(parity)
-        : "memory");
-    if (done) return true;
-    if (global_ns() - t0 > kWaitNs) return false;
-  }
-}
 
 // Segment table of tile (cta j, stage k): starts[rpc4] then ends[rpc4] (u32,
 // relative to ptr[first row of the range]) at offset (j * S + k) * 2 * rpc4.
@@ -209,9 +159,7 @@ spmm_staged_kernel(int64_t rows, int64_t cols, int64_t rows_per_cta, int64_t rpc
     const int64_t cnt = min(stage_cols, cols - lo);
     uint64_t* b = &bar[k & 1];
     const uint32_t opb = (uint32_t)(cnt * ROWB);
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)),
-                 "r"(opb + (uint32_t)seg_bytes)
-                 : "memory");
+    mbar_expect_tx(b, opb + (uint32_t)seg_bytes);
     bulk_copy(ops + (size_t)(k & 1) * stage_bytes, in + lo * B, opb, b);
     bulk_copy(reinterpret_cast<unsigned char*>(segs) + (size_t)(k & 1) * seg_bytes,
               table + (size_t)(blockIdx.x * S + k) * 2 * rpc4, (uint32_t)seg_bytes, b);
