@@ -58,9 +58,12 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--stages", type=int, default=1, help="also time binning and kNN (rank 0)")
     p.add_argument("--bin-cells", type=int, default=5000)
-    p.add_argument("--workload", default="single", choices=["single", "batched", "gradient"],
+    p.add_argument("--workload", default="single", choices=["single", "batched", "gradient", "large", "knn"],
                    help="single: 100k x 500k (default); batched: 64 datasets of 2k-200k cells; "
-                        "gradient: d(sum of top-30 eigenvalues)/d(feature weights) at 200k x 500k")
+                        "gradient: d(sum of top-30 eigenvalues)/d(feature weights) at 200k x 500k; "
+                        "large: 1M x 500k spectral (block 32) + exact kNN k=50; "
+                        "knn: exact kNN k=50 on --cells clustered 30-dim points")
+    p.add_argument("--large-block", type=int, default=32)
     p.add_argument("--fd-directions", type=int, default=4)
     p.add_argument("--datasets", type=int, default=64)
     return p.parse_args()
@@ -254,6 +257,39 @@ def measure_stages(args, dev, ev, U):
     return out
 
 
+def gather_ceiling(csr, block, dev):
+    """Time the row gathers of both SpMM passes alone (sg_gather_ceiling) over
+    this matrix's own index streams: the floor of each pass for this access
+    pattern, reported beside the HBM roofline."""
+    import torch
+    from snapatac2_gb300 import _eigen, _lib
+    L = _lib.lib()
+    op = _eigen.build_operator(csr)
+    n, m, nnz = op.n, op.m, csr.nnz
+    zs = torch.randn(n, block, device=dev)
+    t = torch.randn(m, block, device=dev)
+    sink = torch.zeros(1, device=dev)
+    sh = torch.cuda.current_stream(dev).cuda_stream
+
+    def timed(idx, table):
+        _lib.check(L.sg_gather_ceiling(0, block, nnz, idx.data_ptr(), table.data_ptr(), sink.data_ptr(), sh), "gather")
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(5):
+            L.sg_gather_ceiling(0, block, nnz, idx.data_ptr(), table.data_ptr(), sink.data_ptr(), sh)
+        e1.record()
+        e1.synchronize()
+        return e0.elapsed_time(e1) / 5
+
+    gt, gx = timed(op.rowidx, zs), timed(csr.indices, t)
+    del op
+    rows_per_s = 2 * nnz / ((gt + gx) / 1e3)
+    return {"what": "row gathers of each SpMM pass alone over the same index streams (sg_gather_ceiling): "
+                    "one L1/L2 line per gathered row at block 8 FP32",
+            "xt_gather_ms": gt, "x_gather_ms": gx, "gathered_rows_per_s": rows_per_s,
+            "gathered_GBps": rows_per_s * block * 4 / 1e9}
+
+
 def run_gpu(args):
     import torch
     world, rank, local = dist_env()
@@ -332,6 +368,34 @@ def run_gpu(args):
     achieved = (tb + xb) / max((t_time + x_time) / 1e3, 1e-12) / 1e9
     peak, peak_kind = peaks()
     spmm_share = (t_time + x_time) / (ms * args.steps)
+    gather = gather_ceiling(csr, args.block, dev) if rank == 0 else None
+    if gather is not None:
+        nl = max(len(spmm_ev), 1)
+        gather.update({"xt_spmm_ms": t_time / nl, "x_spmm_ms": x_time / nl,
+                       "frac": (gather["xt_gather_ms"] + gather["x_gather_ms"]) / ((t_time + x_time) / nl)})
+
+    # ---- end to end through the public API (pinned host CSR) ---------------
+    e2e = None
+    if args.e2e_steps > 0:
+        host = DeviceCSR(indptr.cpu().pin_memory(), indices.cpu().pin_memory(), None, (n, m))
+        ad = snap.AnnData(n_obs=n, n_vars=m)
+        ad.X = host
+        h2d = host.indptr.numel() * 8 + host.indices.numel() * 4
+        snap.tl.spectral(ad, features=None, n_comps=args.ncomps, block=args.block)  # warm
+        barrier()
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            snap.tl.spectral(ad, features=None, n_comps=args.ncomps, block=args.block)
+        torch.cuda.synchronize(dev)
+        e2e_ms = (time.perf_counter() - t0) * 1e3 / args.e2e_steps
+        d2h = int(ad.obsm["X_spectral"].size * 8 + ad.uns["spectral_eigenvalue"].size * 8)
+        if world > 1:
+            t = torch.tensor([e2e_ms], device=dev)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            e2e_ms = float(t.item())
+        e2e = {"value": n * world / (e2e_ms / 1e3), "unit": "cells/s", "ms_per_step": e2e_ms,
+               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": d2h}
 
     # ---- FP64 GPU form and accuracy of the mixed result --------------------
     fp64 = accuracy = None
@@ -359,29 +423,6 @@ def run_gpu(args):
                             "reported separately",
                     "lm_set_magnitude_rel_err_max": float(np.max(np.abs(np.sort(np.abs(ev)) - np.sort(np.abs(ev64)))
                                                                  / np.sort(np.abs(ev64))))}
-
-    # ---- end to end through the public API (pinned host CSR) ---------------
-    e2e = None
-    if args.e2e_steps > 0:
-        host = DeviceCSR(indptr.cpu().pin_memory(), indices.cpu().pin_memory(), None, (n, m))
-        ad = snap.AnnData(n_obs=n, n_vars=m)
-        ad.X = host
-        h2d = host.indptr.numel() * 8 + host.indices.numel() * 4
-        snap.tl.spectral(ad, features=None, n_comps=args.ncomps, block=args.block)  # warm
-        barrier()
-        torch.cuda.synchronize(dev)
-        t0 = time.perf_counter()
-        for _ in range(args.e2e_steps):
-            snap.tl.spectral(ad, features=None, n_comps=args.ncomps, block=args.block)
-        torch.cuda.synchronize(dev)
-        e2e_ms = (time.perf_counter() - t0) * 1e3 / args.e2e_steps
-        d2h = int(ad.obsm["X_spectral"].size * 8 + ad.uns["spectral_eigenvalue"].size * 8)
-        if world > 1:
-            t = torch.tensor([e2e_ms], device=dev)
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            e2e_ms = float(t.item())
-        e2e = {"value": n * world / (e2e_ms / 1e3), "unit": "cells/s", "ms_per_step": e2e_ms,
-               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": d2h}
 
     # ---- other stages of the path (rank 0, reported beside the headline) ----
     stages = {}
@@ -422,6 +463,8 @@ def run_gpu(args):
         "gpu_launches": launches,
         "clocks": clk,
     }
+    if gather is not None:
+        line["gather_roofline"] = gather
     if cpu is not None:
         line["cpu_baseline"] = cpu
     if stages:
@@ -552,6 +595,88 @@ def run_gradient(args):
     print(json.dumps(line), flush=True)
 
 
+def run_large(args):
+    """1,000,000 cells x 500,000 features (~4,000 nnz/cell, 4.1e9 nnz, int32
+    indices, implicit 1.0 values): mixed-precision spectral embedding with
+    block size 32, 30 components, then the exact kNN (k = 50) of the
+    weighted embedding.  One timed run after one warm-up (tuning, first
+    allocations); the CSR is resident in HBM before the clock starts."""
+    import torch
+    from snapatac2_gb300 import _eigen, synthetic as syn
+    from snapatac2_gb300._binning import DeviceCSR
+    from snapatac2_gb300._knn_api import knn_arrays
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    n, m = 1_000_000, args.features
+    ip, ix, _ = syn.binary_csr_device(n, m, nnz_per_cell=args.nnz, seed=4242, device=dev)
+    csr = DeviceCSR(ip, ix, None, (n, m))
+    torch.cuda.synchronize(dev)
+
+    def run():
+        t0 = time.perf_counter()
+        op = _eigen.build_operator(csr)
+        torch.cuda.synchronize(dev)
+        t1 = time.perf_counter()
+        res = _eigen.eigsh_lm(op, args.ncomps, block=args.large_block)
+        torch.cuda.synchronize(dev)
+        t2 = time.perf_counter()
+        ev = res.evals
+        pos = np.flatnonzero(ev > 0)
+        E = (res.evecs[:, torch.from_numpy(pos).to(dev)] * torch.from_numpy(np.sqrt(ev[pos])).to(dev)).contiguous()
+        nbr, dist, nfb = knn_arrays(E, 50, return_fallbacks=True)
+        torch.cuda.synchronize(dev)
+        t3 = time.perf_counter()
+        del op
+        return (t1 - t0, t2 - t1, t3 - t2, res.info, int(nfb))
+
+    run()  # warm-up: SpMM tuning, allocator
+    tb, te, tk, info, nfb = run()
+    total = tb + te + tk
+    line = {"metric": "1M-cell spectral (30 comps) + exact kNN k=50, wall seconds", "value": total, "unit": "s",
+            "higher_is_better": False, "n_gpus": 1, "data": "synthetic", "dtype": "f32 (FP64 Rayleigh-Ritz)",
+            "config": {"workload": f"{n} cells x {m} features, nnz {csr.nnz}, block {args.large_block}",
+                       "target_s": 30},
+            "operator_build_s": tb, "eigensolve_s": te, "knn_s": tk, "knn_fp64_rescans": nfb,
+            "block_matvecs": info["block_matvecs"], "restarts": info["restarts"],
+            "phase_seconds": info.get("phase_seconds")}
+    print(json.dumps(line), flush=True)
+
+
+def run_knn(args):
+    """Exact kNN (k = 50) on --cells points in 30 dimensions drawn around 12
+    cluster centres (the shape of a spectral embedding): warm-up calls, then
+    --steps timed calls with CUDA events; the first 64 rows are checked
+    against the oracle's FP64 brute force."""
+    import torch
+    from oracle import knn as oknn
+    from snapatac2_gb300._knn_api import knn_arrays
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    n = args.cells
+    rng = np.random.default_rng(0)
+    centers = rng.standard_normal((12, 30)) * 0.05
+    E = centers[rng.integers(0, 12, n)] + rng.standard_normal((n, 30)) * 0.01
+    Et = torch.from_numpy(E).to(dev)
+    for _ in range(max(args.warmup, 1)):
+        knn_arrays(Et, 50)
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        nbr, dist, nfb = knn_arrays(Et, 50, return_fallbacks=True)
+    e1.record()
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    q = min(n, 64)
+    same = bool(np.array_equal(nbr[:q].cpu().numpy(), oknn.knn_arrays(E, 50, 0, q)[0]))
+    line = {"metric": "exact kNN k=50, queries/s", "value": n / (ms / 1e3), "unit": "queries/s",
+            "higher_is_better": True, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "data": "synthetic", "dtype": "f32 filter, f64 re-rank",
+            "config": {"workload": f"{n} points x 30 dims, 12 clusters, k=50"}, "fp64_rescans": int(nfb),
+            "sample_rows_identical_to_oracle": same}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -560,6 +685,10 @@ def main():
         run_batched(args)
     elif args.workload == "gradient":
         run_gradient(args)
+    elif args.workload == "large":
+        run_large(args)
+    elif args.workload == "knn":
+        run_knn(args)
     else:
         run_gpu(args)
 

@@ -205,6 +205,15 @@ int sg_spmm_staged(int dtype, int block, int64_t rows, int64_t cols, const int64
                    const void* dshift, const void* y, int variant, const unsigned char* row_mask, int* status,
                    void* stream);
 
+/* Diagnostic (no reference counterpart): the row gathers of one SpMM pass  */
+/* alone -- table[idx[e]] (block values per row, same 16-byte vectors and    */
+/* lanes per row as the SpMM) for every e < nnz, folded into registers, no   */
+/* output.  Its time over a matrix's index stream is the floor the SpMM      */
+/* pass can reach with this access pattern.  sink: one float, written only   */
+/* in a case that does not occur for finite tables.                          */
+int sg_gather_ceiling(int dtype, int block, int64_t nnz, const int32_t* idx, const void* table, float* sink,
+                      void* stream);
+
 /* ---- block Krylov-Schur (thick-restart block Lanczos) building blocks --- */
 /* Q: n x ldq row-major basis; W: n x block working block.                   */
 

@@ -4,9 +4,16 @@ Drop-in API (same names, keywords, defaults and output slots as
 ``snapatac2.pp`` / ``snapatac2.tl``):
 
 * ``pp.add_tile_matrix``  -- fragments -> cell x 500 bp tile counts (GPU)
-* ``pp.select_features``  -- most accessible tiles (host NumPy)
+* ``pp.select_features``  -- most accessible tiles (column counts on the GPU,
+                             ranking on the host with NumPy's tie order)
 * ``tl.spectral``         -- matrix-free cosine spectral embedding (GPU)
 * ``pp.knn``              -- exact Euclidean kNN graph (GPU)
+
+Beyond the reference:
+
+* ``spectral_batched``    -- many datasets embedded in one stacked solve
+* ``topk_eigenvalue_sum`` -- sum of the top-k eigenvalues as a differentiable
+                             function of the feature weights (torch.autograd)
 
 All compute goes through ``libsnapgb300.so`` (C ABI in ``include/snapgb300.h``).
 """
@@ -33,6 +40,12 @@ def __getattr__(name):
         ns = _Namespace(spectral=_t.spectral)
         globals()["tl"] = ns
         return ns
+    if name == "spectral_batched":
+        from ._batched import spectral_batched
+        return spectral_batched
+    if name == "topk_eigenvalue_sum":
+        from ._adjoint import topk_eigenvalue_sum
+        return topk_eigenvalue_sum
     raise AttributeError(name)
 
 

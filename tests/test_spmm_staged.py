@@ -116,3 +116,23 @@ def test_staged_spmm_rejects_bad_arguments():
     assert L.sg_spmm_staged(*args(0, 0, buf.data_ptr())) == _lib.SG_ERR_ARG        # no columns
     assert L.sg_spmm_staged(*args(2, 99, buf.data_ptr())) == _lib.SG_ERR_ARG       # no such variant
     assert L.sg_spmm_staged(*args(2, 0, buf.data_ptr() + 4)) == _lib.SG_ERR_ARG    # misaligned operand
+
+
+@pytest.mark.gpu
+def test_gather_ceiling_diagnostic_runs_without_output():
+    import torch
+    L = _lib.lib()
+    dev = torch.device("cuda", 0)
+    indptr, idx, _ = random_csr(2000, 5000, 30, 3, False)
+    d_idx = torch.from_numpy(idx).to(dev)
+    sh = torch.cuda.current_stream(dev).cuda_stream
+    for dtype, tdt in ((0, torch.float32), (1, torch.float64)):
+        for block in (4, 8, 16, 32):
+            table = torch.randn(5000, block, dtype=tdt, device=dev)
+            sink = torch.zeros(1, dtype=torch.float32, device=dev)
+            assert L.sg_gather_ceiling(dtype, block, idx.size, d_idx.data_ptr(), table.data_ptr(), sink.data_ptr(),
+                                       sh) == _lib.SG_OK
+            torch.cuda.synchronize()
+            assert float(sink.item()) == 0.0
+    assert L.sg_gather_ceiling(0, 12, idx.size, d_idx.data_ptr(), table.data_ptr(), sink.data_ptr(), sh) == \
+        _lib.SG_ERR_ARG
