@@ -55,10 +55,18 @@ proj_partial(int64_t n, const T* __restrict__ Q, int64_t ldq, int ncols, const T
     for (int q = 0; q < CPT; ++q) {
       const int p = threadIdx.x + q * kProjBlock;
       if (p < ncols) {
-        for (int i = 0; i < nr; ++i) {
-          const T qv = Q[(base + i) * ldq + p];
+        // several rows' loads in flight, then their FMAs in row order
+        constexpr int RU = B * CPT * (int)sizeof(T) >= 64 ? 2 : 8;
+        for (int i0 = 0; i0 < nr; i0 += RU) {
+          T qv[RU];
 #pragma unroll
-          for (int c = 0; c < B; ++c) acc[q][c] = fma(qv, ws[i][c], acc[q][c]);
+          for (int u = 0; u < RU; ++u) qv[u] = i0 + u < nr ? Q[(base + i0 + u) * ldq + p] : T(0);
+#pragma unroll
+          for (int u = 0; u < RU; ++u)
+            if (i0 + u < nr) {
+#pragma unroll
+              for (int c = 0; c < B; ++c) acc[q][c] = fma(qv[u], ws[i0 + u][c], acc[q][c]);
+            }
         }
       }
     }
@@ -120,16 +128,70 @@ __global__ void __launch_bounds__(256) gram_partial(int64_t n, const T* __restri
   }
 }
 
-__global__ void proj_reduce(int nparts, int ncols, int B, const double* __restrict__ part, double* __restrict__ C) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+// C[t] = sum over the nparts partials of part[b][t], t < tot = ncols * B.  A
+// CTA owns 32 consecutive outputs (lane = output, coalesced reads); warp w
+// sums the partials b = w, w + 32, ... in order, then the 32 warp sums are
+// added in warp order: a fixed order, so the result is deterministic.
+constexpr int kReduceWarps = 32;
+__global__ void __launch_bounds__(kReduceWarps * 32)
+proj_reduce(int nparts, int ncols, int B, const double* __restrict__ part, double* __restrict__ C) {
+  __shared__ double ws[kReduceWarps][33];
   const int tot = ncols * B;
-  if (t >= tot) return;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int t = blockIdx.x * 32 + lane;
   double s = 0.0;
-  for (int b = 0; b < nparts; ++b) s += part[(int64_t)b * tot + t];
-  C[t] = s;
+  if (t < tot) {
+    int b = w;
+    for (; b + 3 * kReduceWarps < nparts; b += 4 * kReduceWarps) {
+      const double v0 = part[(int64_t)b * tot + t], v1 = part[(int64_t)(b + kReduceWarps) * tot + t];
+      const double v2 = part[(int64_t)(b + 2 * kReduceWarps) * tot + t];
+      const double v3 = part[(int64_t)(b + 3 * kReduceWarps) * tot + t];
+      s += v0;
+      s += v1;
+      s += v2;
+      s += v3;
+    }
+    for (; b < nparts; b += kReduceWarps) s += part[(int64_t)b * tot + t];
+  }
+  ws[w][lane] = s;
+  __syncthreads();
+  if (w == 0 && t < tot) {
+    double r = 0.0;
+    for (int k = 0; k < kReduceWarps; ++k) r += ws[k][lane];
+    C[t] = r;
+  }
 }
 
-// W[i,:] -= Q[i, :ncols] C   (one warp per row; lanes over basis columns)
+// W[i,:] -= Q[i, :ncols] C   (one warp per row; lanes over basis columns).
+// Each lane loads up to eight basis entries of the row before using them; the
+// B column sums are then combined by a transpose butterfly (lane pairs swap
+// half of their sums at each step), which leaves each column's full sum in
+// the 32/B lanes whose high bits spell its index, with B - 1 + 5 - log2(B)
+// shuffles instead of 5 B.  Fixed order: deterministic.
+template <typename T, int B>
+__device__ __forceinline__ void warp_colsum(T (&acc)[B], int lane) {
+  // halve the columns a lane holds while doubling the lanes each sum covers
+  int live = B;
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) {
+    if (live > 1) {
+      const int half = live / 2;
+      const bool upper = (lane & o) != 0;
+#pragma unroll
+      for (int c = 0; c < B / 2; ++c) {
+        if (c < half) {
+          const T send = upper ? acc[c] : acc[c + half];
+          const T recv = __shfl_xor_sync(0xffffffffu, send, o);
+          acc[c] = (upper ? acc[c + half] : acc[c]) + recv;
+        }
+      }
+      live = half;
+    } else {
+      acc[0] += __shfl_xor_sync(0xffffffffu, acc[0], o);
+    }
+  }
+}
+
 template <typename T, int B>
 __global__ void __launch_bounds__(256)
 update_kernel(int64_t n, const T* __restrict__ Q, int64_t ldq, int ncols, const double* __restrict__ C,
@@ -145,49 +207,69 @@ update_kernel(int64_t n, const T* __restrict__ Q, int64_t ldq, int ncols, const 
     T acc[B];
 #pragma unroll
     for (int c = 0; c < B; ++c) acc[c] = T(0);
-    for (int p = lane; p < ncols; p += 32) {
-      const T qv = Q[i * ldq + p];
+    for (int p0 = 0; p0 < ncols; p0 += 8 * 32) {
+      T qv[8];
 #pragma unroll
-      for (int c = 0; c < B; ++c) acc[c] = fma(qv, cs[p * B + c], acc[c]);
+      for (int u = 0; u < 8; ++u) {
+        const int p = p0 + u * 32 + lane;
+        qv[u] = p < ncols ? Q[i * ldq + p] : T(0);
+      }
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int p = p0 + u * 32 + lane;
+        if (p < ncols) {
+#pragma unroll
+          for (int c = 0; c < B; ++c) acc[c] = fma(qv[u], cs[p * B + c], acc[c]);
+        }
+      }
     }
+    warp_colsum<T, B>(acc, lane);
+    // the halvings used lane bits 16, 8, ... (B of the 32 lanes' patterns);
+    // the upper half at each step adds half to the column index.  Lanes that
+    // differ only in the remaining low bits hold the same sum; the one with
+    // those bits zero writes it.
+    int col = 0, live = B;
 #pragma unroll
-    for (int c = 0; c < B; ++c) {
-      T v = acc[c];
-#pragma unroll
-      for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-      acc[c] = v;
+    for (int o = 16; o >= 1; o >>= 1) {
+      if (live > 1) {
+        live /= 2;
+        if (lane & o) col += live;
+      }
     }
-    // lane c writes column c (B <= 32)
-    T mine = T(0);
-#pragma unroll
-    for (int c = 0; c < B; ++c) if (lane == c) mine = acc[c];
-    if (lane < B) W[i * B + lane] -= mine;
+    if ((lane % (32 / B)) == 0) W[i * B + col] -= acc[0];
   }
 }
 
 // Cholesky of the B x B Gram matrix (one warp, lane j owns column j):
 // G = RᵀR with R upper triangular; also Rinv = R⁻¹.  A non-positive pivot
-// relative to the diagonal sets SG_ERR_NUMERIC (rank-deficient block).
+// relative to the diagonal sets SG_ERR_NUMERIC (rank-deficient block).  G is
+// staged in shared memory first; lane j's column of R⁻¹ is built in shared
+// memory (no per-thread local arrays).
 __global__ void chol_kernel(int B, const double* __restrict__ G, double* __restrict__ R,
                             double* __restrict__ Rinv, int* status) {
+  __shared__ double g[32][33];
   __shared__ double r[32][33];
+  __shared__ double x[32][33];  // x[i][j]: row i of column j of R⁻¹
   const int j = threadIdx.x;
-  for (int i = 0; i < B; ++i) r[i][j] = 0.0;
+  for (int t = j; t < B * B; t += 32) g[t / B][t % B] = G[t];
+  for (int i = 0; i < B; ++i) {
+    r[i][j] = 0.0;
+    x[i][j] = 0.0;
+  }
   __syncwarp();
   bool fail = false;
   for (int k = 0; k < B; ++k) {
-    double piv = 0.0;
     if (j == k) {
-      double s = G[k * B + k];
+      double s = g[k][k];
       for (int i = 0; i < k; ++i) s -= r[i][k] * r[i][k];
-      const double gkk = G[k * B + k];
+      const double gkk = g[k][k];
       if (!(s > 1e-28 * (gkk > 0 ? gkk : 1.0)) || !(s > 0.0)) { fail = true; s = 1.0; }
       r[k][k] = sqrt(s);
     }
     __syncwarp();
-    piv = r[k][k];
+    const double piv = r[k][k];
     if (j > k && j < B) {
-      double s = G[k * B + j];
+      double s = g[k][j];
       for (int i = 0; i < k; ++i) s -= r[i][k] * r[i][j];
       r[k][j] = s / piv;
     }
@@ -196,24 +278,23 @@ __global__ void chol_kernel(int B, const double* __restrict__ G, double* __restr
   if (__any_sync(0xffffffffu, fail) && j == 0) atomicCAS(status, 0, SG_ERR_NUMERIC);
   // back substitution, lane j computes column j of R^-1
   if (j < B) {
-    double x[32];
-    for (int i = 0; i < 32; ++i) x[i] = 0.0;
-    x[j] = 1.0 / r[j][j];
+    x[j][j] = 1.0 / r[j][j];
     for (int i = j - 1; i >= 0; --i) {
       double s = 0.0;
-      for (int t = i + 1; t <= j; ++t) s += r[i][t] * x[t];
-      x[i] = -s / r[i][i];
+      for (int t = i + 1; t <= j; ++t) s += r[i][t] * x[t][j];
+      x[i][j] = -s / r[i][i];
     }
     for (int i = 0; i < B; ++i) {
-      Rinv[i * B + j] = i <= j ? x[i] : 0.0;
+      Rinv[i * B + j] = i <= j ? x[i][j] : 0.0;
       R[i * B + j] = r[i][j];
     }
   }
 }
 
-// W[i,:] <- W[i,:] Rinv   (warp per row, lane c computes column c)
+// W[i,:] <- W[i,:] Rinv for blocks of 16 or 32 (warp per row, lane c
+// computes column c: W[i,k] Rinv[k,c] over k = 0..c in order)
 template <typename T, int B>
-__global__ void __launch_bounds__(256) apply_rinv(int64_t n, const double* __restrict__ Rinv, T* __restrict__ W) {
+__global__ void __launch_bounds__(256) apply_rinv_warp(int64_t n, const double* __restrict__ Rinv, T* __restrict__ W) {
   __shared__ T ri[B][B];
   for (int t = threadIdx.x; t < B * B; t += blockDim.x) ri[t / B][t % B] = (T)Rinv[t];
   __syncthreads();
@@ -229,6 +310,28 @@ __global__ void __launch_bounds__(256) apply_rinv(int64_t n, const double* __res
       if (lane < B && k <= lane) s = fma(wk, ri[k][lane < B ? lane : 0], s);
     }
     if (lane < B) W[i * B + lane] = s;
+  }
+}
+
+// W[i,:] <- W[i,:] Rinv for blocks of 4 or 8 (thread per row, same order)
+template <typename T, int B>
+__global__ void __launch_bounds__(256) apply_rinv(int64_t n, const double* __restrict__ Rinv, T* __restrict__ W) {
+  __shared__ T ri[B][B];
+  for (int t = threadIdx.x; t < B * B; t += blockDim.x) ri[t / B][t % B] = (T)Rinv[t];
+  __syncthreads();
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    T w[B], o[B];
+#pragma unroll
+    for (int k = 0; k < B; ++k) w[k] = W[i * B + k];
+#pragma unroll
+    for (int c = 0; c < B; ++c) {
+      T s = T(0);
+#pragma unroll
+      for (int k = 0; k <= c; ++k) s = fma(w[k], ri[k][c], s);
+      o[c] = s;
+    }
+#pragma unroll
+    for (int c = 0; c < B; ++c) W[i * B + c] = o[c];
   }
 }
 
@@ -322,7 +425,7 @@ int proj_t(int64_t n, const T* Q, int64_t ldq, int ncols, const T* W, double* pa
     else proj_partial<T, B, 2><<<nparts, kProjBlock, 0, s>>>(n, Q + c0, ldq, nc, W, part);
     SG_CHECK_LAUNCH();
     const int tot = nc * B;
-    proj_reduce<<<(tot + 255) / 256, 256, 0, s>>>(nparts, nc, B, part, C + (int64_t)c0 * B);
+    proj_reduce<<<(tot + 31) / 32, kReduceWarps * 32, 0, s>>>(nparts, nc, B, part, C + (int64_t)c0 * B);
     SG_CHECK_LAUNCH();
   }
   return SG_OK;
@@ -364,12 +467,13 @@ int update_dispatch(int B, int64_t n, const T* Q, int64_t ldq, int ncols, const 
 
 template <typename T>
 int rinv_dispatch(int B, int64_t n, const double* Rinv, T* W, cudaStream_t s) {
-  const int grid = grid_for(n * 32, 256, 8 * sm_count_l());
+  const int grid = grid_for(n, 256, 16 * sm_count_l());
+  const int gridw = grid_for(n * 32, 256, 8 * sm_count_l());
   switch (B) {
     case 4: apply_rinv<T, 4><<<grid, 256, 0, s>>>(n, Rinv, W); break;
     case 8: apply_rinv<T, 8><<<grid, 256, 0, s>>>(n, Rinv, W); break;
-    case 16: apply_rinv<T, 16><<<grid, 256, 0, s>>>(n, Rinv, W); break;
-    case 32: apply_rinv<T, 32><<<grid, 256, 0, s>>>(n, Rinv, W); break;
+    case 16: apply_rinv_warp<T, 16><<<gridw, 256, 0, s>>>(n, Rinv, W); break;
+    case 32: apply_rinv_warp<T, 32><<<gridw, 256, 0, s>>>(n, Rinv, W); break;
     default: return SG_ERR_ARG;
   }
   SG_CHECK_LAUNCH();
@@ -427,7 +531,7 @@ extern "C" int sg_block_cholqr(int dtype, int block, int64_t n, void* W, double*
   if (e) return e;
   if (block == 4 || block == 8) {
     SG_CHECK_LAUNCH();
-    proj_reduce<<<(block * block + 255) / 256, 256, 0, s>>>(nparts, block, block, part, G);
+    proj_reduce<<<(block * block + 31) / 32, kReduceWarps * 32, 0, s>>>(nparts, block, block, part, G);
     SG_CHECK_LAUNCH();
   }
   chol_kernel<<<1, 32, 0, s>>>(block, G, R, Rinv, status);
