@@ -27,7 +27,10 @@
 //  4. exact   the same scan in FP64 for the queued queries only.
 //  5. rows sorted by column index, distances sqrt'ed.
 // Ties are broken by the smaller index.
+#include <cuda_bf16.h>
 #include <float.h>
+#include <stdlib.h>
+#include <string.h>
 
 #include <type_traits>
 
@@ -110,7 +113,7 @@ template <typename TD, int DP>
 __global__ void __launch_bounds__(kLW * 32)
 scan_kernel(const TD* __restrict__ Xp, int64_t n, const int* __restrict__ qlist, const int* __restrict__ qcount,
             int Kp, int* __restrict__ cand, TD* __restrict__ cand_d, TD* __restrict__ tau_out) {
-  extern __shared__ __align__(16) unsigned char sraw[];
+  extern __shared__ __align__(128) unsigned char sraw[];
   ScanSmem<TD, DP>& sm = *reinterpret_cast<ScanSmem<TD, DP>*>(sraw);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int64_t nq = qcount ? (int64_t)*qcount : n;
@@ -268,7 +271,7 @@ template <int DP, int LIST>
 __global__ void __launch_bounds__(kFW * 32, 2)
 filter_scan_kernel(const float* __restrict__ XT, const float* __restrict__ nrm, int64_t n, int d, int Kp,
                    int* __restrict__ cand, float* __restrict__ tau_out) {
-  extern __shared__ __align__(16) unsigned char sraw[];
+  extern __shared__ __align__(128) unsigned char sraw[];
   FilterSmem<DP, LIST>& sm = *reinterpret_cast<FilterSmem<DP, LIST>*>(sraw);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int64_t qbase = (int64_t)blockIdx.x * kFQ;
@@ -439,6 +442,283 @@ filter_scan_kernel(const float* __restrict__ XT, const float* __restrict__ nrm, 
   if (threadIdx.x == 0 && failed)
     for (int64_t t = issued - kFBuf < 0 ? 0 : issued - kFBuf; t < issued; ++t)
       mbar_wait(&sm.full[t % kFBuf], (uint32_t)((t / kFBuf) & 1));
+}
+
+// ---------------------------------------------------------------------------
+// Tensor-core filter (d <= 32).  The filter's dot products q.c come from
+// tcgen05.mma: the centred FP32 coordinates are split into bf16 hi + lo and
+// q.c ~= qh.ch + qh.cl + ql.ch (three K = 32 products per 128 x 128 tile,
+// FP32 accumulation in TMEM).  Dropped terms and accumulation stay below
+// 6e-5 sum|q_t c_t|; the filter is widened by KTC = 2^-12 of nq + nc (four
+// times that), so, as in the FP32 filter, no pair whose difference-form
+// distance is below tau is dropped; the verify, the lists and the output are
+// those of filter_scan_kernel.
+//
+// TC layout (prep): per 128-point tile, [hi 8 KB][lo 8 KB][nc (1 - K) 512 B],
+// hi and lo in the no-swizzle K-major core-matrix layout: element (row r,
+// dim t) at byte (r/8)*512 + (t/8)*128 + (r%8)*16 + (t%8)*2.
+// ---------------------------------------------------------------------------
+constexpr int kTQ = 128;                  // queries per CTA (MMA M)
+constexpr int kTC = 128;                  // candidates per tile (MMA N)
+constexpr int kTDim = 32;                 // K (padded dimensions)
+constexpr int kTMat = kTQ * kTDim * 2;    // one bf16 operand: 8 KB
+constexpr int kTTile = 2 * kTMat + kTC * 4;  // hi, lo, norms
+constexpr int kTBuf = 3;
+constexpr int kTList = 128;               // Kp + 16 <= 128
+constexpr int kTChunk = 16;               // candidates per thread between verify rounds
+constexpr int kTQueue = 32 * kTChunk;     // per consumer warp
+constexpr int kTConsumers = 4;            // warps 0..3 read TMEM lanes 32w..32w+31
+constexpr int kTThreads = (kTConsumers + 1) * 32;  // + one producer warp
+constexpr float kTcK = 2.44140625e-4f + 8.0f * 5.9604644775390625e-08f;  // 2^-12 + rounding of the test
+
+struct TcSmem {
+  uint64_t full[kTBuf];     // tile landed
+  uint64_t sfree[kTBuf];    // tile consumed: MMA done (commit) + 4 consumer warps
+  uint64_t mdone[2];        // accumulator buffer x holds tile k (commit)
+  uint64_t tfree[2];        // accumulator buffer x read by the 4 consumer warps
+  uint64_t aful;            // query operands landed
+  uint32_t tmem_slot;
+  int failed;
+  __align__(128) unsigned char A[2 * kTMat];
+  __align__(128) unsigned char Bt[kTBuf][kTTile];
+  float qT[kTDim][kTQ];
+  float lk[kTQ][kTList];
+  int li[kTQ][kTList];
+  int cnt[kTQ];
+  float tau[kTQ];
+  unsigned queue[kTConsumers][kTQueue];
+  int nqueue[kTConsumers];
+};
+
+__device__ __forceinline__ uint32_t tc_off(int r, int t) {
+  return (uint32_t)((r >> 3) * 512 + (t >> 3) * 128 + (r & 7) * 16 + (t & 7) * 2);
+}
+
+// TC layout from the tile-transposed FP32 copy (XT) and the norms.
+__global__ void tc_prep_kernel(const float* __restrict__ XT, const float* __restrict__ nrm, int64_t n,
+                               unsigned char* __restrict__ TC) {
+  const int64_t npad = (n + kFC - 1) / kFC * kFC;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < npad; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t k = i / kFC;
+    const int r = (int)(i % kFC);
+    unsigned char* tile = TC + k * kTTile;
+    const float* src = XT + k * 32 * kFC + r;
+    for (int t = 0; t < kTDim; ++t) {
+      const float v = src[t * kFC];
+      const __nv_bfloat16 h = __float2bfloat16_rn(v);
+      const __nv_bfloat16 l = __float2bfloat16_rn(v - __bfloat162float(h));
+      *reinterpret_cast<__nv_bfloat16*>(tile + tc_off(r, t)) = h;
+      *reinterpret_cast<__nv_bfloat16*>(tile + kTMat + tc_off(r, t)) = l;
+    }
+    reinterpret_cast<float*>(tile + 2 * kTMat)[r] = nrm[i] * (1.0f - kTcK);  // the filter's nc (1 - K)
+  }
+}
+
+__global__ void __launch_bounds__(kTThreads, 1)
+tc_filter_kernel(const float* __restrict__ XT, const unsigned char* __restrict__ TC, const float* __restrict__ nrm,
+                 int64_t n, int d, int Kp, int* __restrict__ cand, float* __restrict__ tau_out) {
+  extern __shared__ __align__(128) unsigned char sraw[];
+  TcSmem& sm = *reinterpret_cast<TcSmem*>(sraw);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int64_t qbase = (int64_t)blockIdx.x * kTQ;
+  const int64_t ntiles = (n + kTC - 1) / kTC;
+  if (wid == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;" ::"r"(smem_u32(&sm.tmem_slot)));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (threadIdx.x == 0) {
+    for (int b = 0; b < kTBuf; ++b) {
+      mbar_init(&sm.full[b], 1);
+      mbar_init(&sm.sfree[b], 1 + kTConsumers);
+    }
+    for (int x = 0; x < 2; ++x) {
+      mbar_init(&sm.mdone[x], 1);
+      mbar_init(&sm.tfree[x], kTConsumers);
+    }
+    mbar_init(&sm.aful, 1);
+    sm.failed = 0;
+    fence_barrier_init();
+  }
+  if (wid < kTConsumers) {
+    const float* src = XT + (qbase / kFC) * 32 * kFC;
+    for (int e = threadIdx.x; e < kTDim * kTQ; e += kTConsumers * 32) sm.qT[e / kTQ][e % kTQ] = src[e];
+    if (lane < 32) {
+      sm.cnt[wid * 32 + lane] = 0;
+      sm.tau[wid * 32 + lane] = FLT_MAX;
+    }
+    if (lane == 0) sm.nqueue[wid] = 0;
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = sm.tmem_slot;
+  const uint32_t idesc = umma_idesc_bf16(kTQ, kTC);
+  bool failed = false;
+
+  if (wid == kTConsumers) {
+    // ---------------- producer: tile copies and MMAs (one thread) ---------
+    if (lane == 0) {
+      auto issue = [&](int64_t k) {
+        const int b = (int)(k % kTBuf);
+        mbar_expect_tx(&sm.full[b], kTTile);
+        bulk_copy(sm.Bt[b], TC + k * kTTile, kTTile, &sm.full[b]);
+      };
+      mbar_expect_tx(&sm.aful, 2 * kTMat);
+      bulk_copy(sm.A, TC + (qbase / kFC) * kTTile, 2 * kTMat, &sm.aful);
+      for (int64_t k = 0; k < 2 && k < ntiles; ++k) issue(k);
+      bool ok = mbar_wait(&sm.aful, 0);
+      const uint32_t a_hi = smem_u32(sm.A), a_lo = a_hi + kTMat;
+      // tile k: MMA as soon as it landed and its accumulator buffer was read
+      // out (tile k - 2); then refill the buffer tile k - 1 used with tile
+      // k + 2 once the consumers are done with tile k - 1.  The tensor cores
+      // thus work on tile k + 1 while the consumers filter tile k.
+      for (int64_t k = 0; ok && k < ntiles; ++k) {
+        const int b = (int)(k % kTBuf), x = (int)(k & 1);
+        ok = mbar_wait(&sm.full[b], (uint32_t)((k / kTBuf) & 1));
+        if (ok && k >= 2) ok = mbar_wait(&sm.tfree[x], (uint32_t)(((k / 2) - 1) & 1));
+        if (!ok) break;
+        tc_fence_after();
+        const uint32_t b_hi = smem_u32(sm.Bt[b]), b_lo = b_hi + kTMat;
+        const uint32_t dst = tmem + (uint32_t)(x * kTC);
+        const uint32_t pa[3] = {a_hi, a_hi, a_lo}, pb[3] = {b_hi, b_lo, b_hi};
+#pragma unroll
+        for (int p = 0; p < 3; ++p)
+#pragma unroll
+          for (int ks = 0; ks < kTDim / 16; ++ks)
+            umma_bf16(dst, umma_desc(pa[p] + ks * 256u, 128u, 512u), umma_desc(pb[p] + ks * 256u, 128u, 512u), idesc,
+                      p > 0 || ks > 0);
+        umma_commit(&sm.mdone[x]);
+        umma_commit(&sm.sfree[b]);
+        const int64_t kt = k + 2;
+        if (kt < ntiles) {
+          if (k >= 1) ok = mbar_wait(&sm.sfree[(k - 1) % kTBuf], (uint32_t)(((k - 1) / kTBuf) & 1));
+          if (!ok) break;
+          fence_proxy_async();
+          issue(kt);
+        }
+      }
+      if (!ok) atomicExch(&sm.failed, 1);
+    }
+  } else {
+    // ---------------- consumers: filter from TMEM, verify, lists ----------
+    const int row = wid * 32 + lane;
+    const int64_t q = qbase + row;
+    const float nq = q < n ? nrm[q] : 0.f;
+    const float u = 5.9604644775390625e-08f;
+    const float Tu = (float)(4 * (d + 4)) * u;
+    const float kInf = __int_as_float(0x7f800000);
+    for (int64_t k = 0; k < ntiles; ++k) {
+      const int b = (int)(k % kTBuf), x = (int)(k & 1);
+      bool ok = mbar_wait(&sm.mdone[x], (uint32_t)((k / 2) & 1));
+      ok = ok && mbar_wait(&sm.full[b], (uint32_t)((k / kTBuf) & 1));  // the norms of this tile
+      if (!__all_sync(0xffffffffu, ok)) {
+        failed = true;
+        break;
+      }
+      tc_fence_after();
+      float sacc[kTC];
+#pragma unroll
+      for (int c0 = 0; c0 < kTC; c0 += 32) {
+        float v[32];
+        tmem_ld32(tmem + ((uint32_t)(wid * 32) << 16) + (uint32_t)(x * kTC + c0), v);
+#pragma unroll
+        for (int j = 0; j < 32; ++j) sacc[c0 + j] = v[j];
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&sm.tfree[x]);  // accumulator buffer x may be overwritten
+      const int64_t c0 = k * kTC;
+      const float4* cadj4 = reinterpret_cast<const float4*>(sm.Bt[b] + 2 * kTMat);
+      const float tq = sm.tau[row];
+      const float T = q >= n ? -kInf : (tq >= FLT_MAX ? kInf : (tq + Tu * tq) + (kTcK * nq - nq));
+      // acceptance mask of the 128 candidates (the query's own column is
+      // removed in the verify step)
+      uint32_t m0 = 0, m1 = 0, m2 = 0, m3 = 0;
+#pragma unroll
+      for (int j4 = 0; j4 < kTC / 4; ++j4) {
+        const float4 c = cadj4[j4];
+        const float ca[4] = {c.x, c.y, c.z, c.w};
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          const int j = 4 * j4 + e;
+          const uint32_t bit = fmaf(-2.0f, sacc[j], ca[e]) < T ? 1u : 0u;
+          if (j < 32) m0 |= bit << j;
+          else if (j < 64) m1 |= bit << (j - 32);
+          else if (j < 96) m2 |= bit << (j - 64);
+          else m3 |= bit << (j - 96);
+        }
+      }
+      // drain the masks in rounds of at most kTChunk pairs per lane
+#pragma unroll 1
+      while (__any_sync(0xffffffffu, (m0 | m1 | m2 | m3) != 0)) {
+        int mine = 0;
+#pragma unroll 1
+        while (mine < kTChunk && (m0 | m1 | m2 | m3)) {
+          int j;
+          if (m0) { j = __ffs(m0) - 1; m0 &= m0 - 1; }
+          else if (m1) { j = 32 + __ffs(m1) - 1; m1 &= m1 - 1; }
+          else if (m2) { j = 64 + __ffs(m2) - 1; m2 &= m2 - 1; }
+          else { j = 96 + __ffs(m3) - 1; m3 &= m3 - 1; }
+          sm.queue[wid][atomicAdd(&sm.nqueue[wid], 1)] = ((unsigned)lane << 16) | (unsigned)j;
+          ++mine;
+        }
+        // make room: re-sort the lists that this round could overflow
+        unsigned need = __ballot_sync(0xffffffffu, sm.cnt[row] + mine > kTList);
+        while (need) {
+          const int l = __ffs(need) - 1;
+          need &= need - 1;
+          const int r = wid * 32 + l;
+          merge_list_f<kTList>(sm.lk[r], sm.li[r], &sm.cnt[r], &sm.tau[r], Kp);
+        }
+        __syncwarp();
+        const int nk = sm.nqueue[wid];
+        for (int e = lane; e < nk; e += 32) {
+          const unsigned pr = sm.queue[wid][e];
+          const int r = wid * 32 + (int)(pr >> 16), c = (int)(pr & 0xffffu);
+          if (c0 + c == qbase + r) continue;  // the query itself
+          const float* cx = XT + k * 32 * kFC + c;
+          float dd = 0.f;
+#pragma unroll
+          for (int t = 0; t < kTDim; ++t) {
+            const float df = sm.qT[t][r] - __ldg(cx + t * kFC);
+            dd = fmaf(df, df, dd);
+          }
+          if (dd < sm.tau[r]) {
+            const int p = atomicAdd(&sm.cnt[r], 1);
+            sm.lk[r][p] = dd;
+            sm.li[r][p] = (int)(c0 + c);
+          }
+        }
+        __syncwarp();
+        if (lane == 0) sm.nqueue[wid] = 0;
+        __syncwarp();
+      }
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&sm.sfree[b]);  // done with this tile's norms
+    }
+    failed = __any_sync(0xffffffffu, failed);
+    for (int l = 0; l < 32; ++l) {
+      const int r = wid * 32 + l;
+      const int64_t qq = qbase + r;
+      if (!failed) merge_list_f<kTList>(sm.lk[r], sm.li[r], &sm.cnt[r], &sm.tau[r], Kp);
+      if (qq < n) {
+        const int c = failed ? 0 : sm.cnt[r];
+        for (int t = lane; t < Kp; t += 32) cand[qq * Kp + t] = t < c ? sm.li[r][t] : -1;
+        if (lane == 0) tau_out[qq] = failed ? -1.0f : sm.tau[r];  // negative tau: certificate fails
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  // a producer failure leaves every consumer result to the exact rescan
+  if (sm.failed && wid < kTConsumers) {
+    for (int l = 0; l < 32; ++l) {
+      const int64_t qq = qbase + wid * 32 + l;
+      if (qq < n && lane == 0) tau_out[qq] = -1.0f;
+    }
+  }
+  tc_fence_after();
+  if (wid == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;" ::"r"(tmem));
 }
 
 constexpr int kMeanParts = 256;
@@ -612,6 +892,7 @@ struct KnnScratch {
   double* mean;
   float* XT;
   float* nrm;
+  unsigned char* TC;  // tensor-core operand tiles (DP == 32 only)
   double* X64;
   int* cand;
   float* tau32;
@@ -631,7 +912,8 @@ KnnScratch knn_layout(char* base, int64_t n, int DP, int k, int Kp) {
   auto take = [&](int64_t b) { int64_t r = o; o += align256(b); return r; };
   const int64_t npad = (n + kFC - 1) / kFC * kFC;
   const int64_t omp = take((int64_t)kMeanParts * 64 * 8), omean = take(64 * 8);
-  const int64_t oXT = take(npad * DP * 4), onrm = take(npad * 4), oX64 = take(n * DP * 8),
+  const int64_t oXT = take(npad * DP * 4), onrm = take(npad * 4),
+                oTC = DP == 32 ? take(npad / kFC * kTTile) : 0, oX64 = take(n * DP * 8),
                 oc = take(n * (int64_t)Kp * 4),
                 ot = take(n * 4), of = take(n * 4), ofc = take(n * (int64_t)k * 4),
                 ofd = take(n * (int64_t)k * 8), on = take(16);
@@ -640,6 +922,7 @@ KnnScratch knn_layout(char* base, int64_t n, int DP, int k, int Kp) {
     s.mean = (double*)(base + omean);
     s.XT = (float*)(base + oXT);
     s.nrm = (float*)(base + onrm);
+    s.TC = DP == 32 ? (unsigned char*)(base + oTC) : nullptr;
     s.X64 = (double*)(base + oX64);
     s.cand = (int*)(base + oc);
     s.tau32 = (float*)(base + ot);
@@ -686,6 +969,25 @@ int launch_filter_scan(const float* XT, const float* nrm, int64_t n, int d, int 
   return launch_filter_scan_l<DP, 256>(XT, nrm, n, d, Kp, cand, tau, s);
 }
 
+// The tensor-core filter serves up to 32 dimensions and lists of Kp + one
+// chunk; SNAPGB300_KNN_FILTER=simt selects the FP32 filter (both give the
+// same candidate lists).
+bool use_tensor_filter(int DP, int Kp) {
+  if (DP != 32 || Kp + kTChunk > kTList) return false;
+  const char* e = getenv("SNAPGB300_KNN_FILTER");
+  return !(e && strcmp(e, "simt") == 0);
+}
+
+int launch_tc_filter(const float* XT, const unsigned char* TC, const float* nrm, int64_t n, int d, int Kp, int* cand,
+                     float* tau, cudaStream_t s) {
+  const size_t smem = sizeof(TcSmem);
+  if (cudaFuncSetAttribute(tc_filter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    return SG_ERR_CUDA;
+  const int64_t grid = (n + kTQ - 1) / kTQ;
+  tc_filter_kernel<<<(unsigned)grid, kTThreads, smem, s>>>(XT, TC, nrm, n, d, Kp, cand, tau);
+  return cudaGetLastError() == cudaSuccess ? SG_OK : SG_ERR_CUDA;
+}
+
 template <int DP>
 int knn_run(const double* X, int64_t n, int d, int k, int Kp, const KnnScratch& w, int64_t* nbr, double* dist,
             cudaStream_t s) {
@@ -694,7 +996,14 @@ int knn_run(const double* X, int64_t n, int d, int k, int Kp, const KnnScratch& 
   mean_reduce<<<1, 64, 0, s>>>(w.mpart, kMeanParts, n, d, w.mean);
   prep_kernel<DP><<<grid_for(n, 256, 4096), 256, 0, s>>>(X, n, d, w.mean, w.XT, w.nrm, w.X64, w.maxnorm);
   SG_CHECK_LAUNCH();
-  int e = launch_filter_scan<DP>(w.XT, w.nrm, n, d, Kp, w.cand, w.tau32, s);
+  int e;
+  if (use_tensor_filter(DP, Kp)) {
+    tc_prep_kernel<<<grid_for(n, 256, 4096), 256, 0, s>>>(w.XT, w.nrm, n, w.TC);
+    SG_CHECK_LAUNCH();
+    e = launch_tc_filter(w.XT, w.TC, w.nrm, n, d, Kp, w.cand, w.tau32, s);
+  } else {
+    e = launch_filter_scan<DP>(w.XT, w.nrm, n, d, Kp, w.cand, w.tau32, s);
+  }
   if (e) return e;
   rerank_kernel<DP><<<(unsigned)((n + 7) / 8), 256, 0, s>>>(w.X64, n, d, w.mean, w.cand, Kp, w.tau32, k,
                                                             w.maxnorm, nbr, dist, w.flagged, w.nflag);
@@ -763,12 +1072,12 @@ constexpr int kNoAllocMaxK = 100;        // neighbours
 constexpr int64_t kA256(int64_t x) { return (x + 255) / 256 * 256; }
 // knn_layout(kNoAllocMaxN, 32, kNoAllocMaxK, kMaxKp) written out (kNoAllocMaxN is
 // a multiple of the 128-point tile): mean partials, mean, tile-transposed
-// FP32 points, their norms, X64, candidates, tau, flagged, fallback
-// candidates and distances, counters
+// FP32 points, their norms, tensor-core operand tiles, X64, candidates, tau,
+// flagged, fallback candidates and distances, counters
 static_assert(kNoAllocMaxN % kFC == 0, "no-alloc capacity must be whole tiles");
 constexpr int64_t kNoAllocBytes =
     kA256((int64_t)kMeanParts * 64 * 8) + kA256(64 * 8) + kA256(kNoAllocMaxN * kNoAllocMaxDim * 4) +
-    kA256(kNoAllocMaxN * 4) + kA256(kNoAllocMaxN * kNoAllocMaxDim * 8) +
+    kA256(kNoAllocMaxN * 4) + kA256(kNoAllocMaxN / kFC * kTTile) + kA256(kNoAllocMaxN * kNoAllocMaxDim * 8) +
     kA256(kNoAllocMaxN * kMaxKp * 4) + kA256(kNoAllocMaxN * 4) + kA256(kNoAllocMaxN * 4) +
     kA256(kNoAllocMaxN * kNoAllocMaxK * 4) + kA256(kNoAllocMaxN * kNoAllocMaxK * 8) + kA256(16);
 

@@ -129,3 +129,33 @@ def test_knn_api():
     assert (G2 != want).nnz == 0
     with pytest.raises(ValueError):
         snap.pp.knn(np.zeros((0, 3)))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("filt", ["tensor", "simt"])
+@pytest.mark.parametrize("case", ["single_tile", "partial_tile", "clustered", "lattice_ties", "wide_k", "d17"])
+def test_gpu_filters_match_oracle(filt, case, monkeypatch):
+    """The tensor-core filter (tcgen05 split-BF16 dot products, d <= 32) and
+    the FP32 filter give the oracle's graph; ragged tiles, ties, clusters."""
+    if filt == "simt":
+        monkeypatch.setenv("SNAPGB300_KNN_FILTER", "simt")
+    else:
+        monkeypatch.delenv("SNAPGB300_KNN_FILTER", raising=False)
+    rng = np.random.default_rng(len(case))
+    if case == "single_tile":
+        X, k = rng.standard_normal((100, 20)), 10
+    elif case == "partial_tile":
+        X, k = rng.standard_normal((1000, 30)) * rng.uniform(0.1, 10, 30), 50
+    elif case == "clustered":
+        c = rng.standard_normal((6, 30)) * 0.05
+        X, k = c[rng.integers(0, 6, 6000)] + rng.standard_normal((6000, 30)) * 1e-3, 50
+    elif case == "lattice_ties":
+        X, k = rng.integers(0, 3, (3000, 32)).astype(float), 20
+    elif case == "wide_k":  # k + margin past the tensor path's list: FP32 filter either way
+        X, k = rng.standard_normal((3000, 30)), 100
+    else:
+        X, k = rng.standard_normal((4097, 17)), 60
+    want_n, want_d = oknn.knn_arrays(X, k)
+    nbr, dist, _ = _gpu(X, k)
+    assert np.array_equal(nbr, want_n)
+    assert np.array_equal(dist, want_d)
