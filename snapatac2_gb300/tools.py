@@ -10,6 +10,8 @@ from __future__ import annotations
 
 from typing import Literal
 
+import warnings
+
 import numpy as np
 import scipy.sparse as sp
 import torch
@@ -72,6 +74,10 @@ def spectral_embedding(X, features=None, n_comps: int = 30, random_state: int = 
     csr = _eigen.select_columns(csr, features)
     op = _eigen.build_operator(csr, feature_weights)
     res = _eigen.eigsh_lm(op, n_comps, precision=precision, block=block, seed=random_state, **solver_kw)
+    if not res.info["converged"]:
+        warnings.warn(f"spectral embedding did not reach the requested accuracy "
+                      f"(max residual {max(res.info['residuals']):.2e}, {res.info['restarts']} restarts)",
+                      RuntimeWarning, stacklevel=2)
     if return_info:
         return res.evals, res.evecs, res.info
     return res.evals, res.evecs.cpu().numpy()

@@ -256,3 +256,13 @@ def test_gpu_rejects_duplicate_columns():
     ix = torch.tensor([0, 2, 2, 1, 3], dtype=torch.int32, device=dev)  # row 0 repeats column 2
     with pytest.raises(ValueError):
         _eigen.build_operator(DeviceCSR(ip, ix, None, (2, 4)))
+
+
+@pytest.mark.gpu
+def test_gpu_unconverged_solve_warns():
+    """A solve stopped before the requested accuracy says so (RuntimeWarning)."""
+    from snapatac2_gb300.tools import spectral_embedding
+    B = syn.binary_csr(3000, 20000, nnz_per_cell=200, n_clusters=4, enriched=3000, seed=2)
+    X = sp.csr_matrix((np.ones(B.nnz), B.indices, B.indptr), shape=B.shape)
+    with pytest.warns(RuntimeWarning, match="did not reach"):
+        spectral_embedding(X, None, 30, 0, precision="mixed", max_restarts=0, tol_vec=1e-15, tol_val=1e-15)
