@@ -454,16 +454,19 @@ filter_scan_kernel(const float* __restrict__ XT, const float* __restrict__ nrm, 
 // distance is below tau is dropped; the verify, the lists and the output are
 // those of filter_scan_kernel.
 //
-// TC layout (prep): per 128-point tile, [hi 8 KB][lo 8 KB][nc (1 - K) 512 B],
-// hi and lo in the no-swizzle K-major core-matrix layout: element (row r,
-// dim t) at byte (r/8)*512 + (t/8)*128 + (r%8)*16 + (t%8)*2.
+// TC layout (prep): per 128-point tile, [hi 8 KB][lo 8 KB][lo2 8 KB]
+// [nc (1 - K) 512 B], each bf16 array in the no-swizzle K-major core-matrix
+// layout: element (row r, dim t) at byte (r/8)*512 + (t/8)*128 + (r%8)*16 +
+// (t%8)*2.  hi = RN(v), lo = RN(v - hi), lo2 = RN(v - hi - lo) (bf16): the
+// remainders have at most 16 and 8 significant bits, so hi + lo + lo2 == v
+// exactly and the verify reads exact FP32 coordinates from shared memory.
 // ---------------------------------------------------------------------------
 constexpr int kTQ = 128;                  // queries per CTA (MMA M)
 constexpr int kTC = 128;                  // candidates per tile (MMA N)
 constexpr int kTDim = 32;                 // K (padded dimensions)
 constexpr int kTMat = kTQ * kTDim * 2;    // one bf16 operand: 8 KB
-constexpr int kTTile = 2 * kTMat + kTC * 4;  // hi, lo, norms
-constexpr int kTBuf = 3;
+constexpr int kTTile = 3 * kTMat + kTC * 4;  // hi, lo, lo2, scaled norms
+constexpr int kTBuf = 2;
 constexpr int kTList = 128;               // Kp + 16 <= 128
 constexpr int kTChunk = 16;               // candidates per thread between verify rounds
 constexpr int kTQueue = 32 * kTChunk;     // per consumer warp
@@ -506,11 +509,14 @@ __global__ void tc_prep_kernel(const float* __restrict__ XT, const float* __rest
     for (int t = 0; t < kTDim; ++t) {
       const float v = src[t * kFC];
       const __nv_bfloat16 h = __float2bfloat16_rn(v);
-      const __nv_bfloat16 l = __float2bfloat16_rn(v - __bfloat162float(h));
+      const float r1 = v - __bfloat162float(h);
+      const __nv_bfloat16 l = __float2bfloat16_rn(r1);
+      const __nv_bfloat16 l2 = __float2bfloat16_rn(r1 - __bfloat162float(l));
       *reinterpret_cast<__nv_bfloat16*>(tile + tc_off(r, t)) = h;
       *reinterpret_cast<__nv_bfloat16*>(tile + kTMat + tc_off(r, t)) = l;
+      *reinterpret_cast<__nv_bfloat16*>(tile + 2 * kTMat + tc_off(r, t)) = l2;
     }
-    reinterpret_cast<float*>(tile + 2 * kTMat)[r] = nrm[i] * (1.0f - kTcK);  // the filter's nc (1 - K)
+    reinterpret_cast<float*>(tile + 3 * kTMat)[r] = nrm[i] * (1.0f - kTcK);  // the filter's nc (1 - K)
   }
 }
 
@@ -565,13 +571,13 @@ tc_filter_kernel(const float* __restrict__ XT, const unsigned char* __restrict__
       };
       mbar_expect_tx(&sm.aful, 2 * kTMat);
       bulk_copy(sm.A, TC + (qbase / kFC) * kTTile, 2 * kTMat, &sm.aful);
-      for (int64_t k = 0; k < 2 && k < ntiles; ++k) issue(k);
+      for (int64_t k = 0; k < kTBuf && k < ntiles; ++k) issue(k);
       bool ok = mbar_wait(&sm.aful, 0);
       const uint32_t a_hi = smem_u32(sm.A), a_lo = a_hi + kTMat;
       // tile k: MMA as soon as it landed and its accumulator buffer was read
       // out (tile k - 2); then refill the buffer tile k - 1 used with tile
-      // k + 2 once the consumers are done with tile k - 1.  The tensor cores
-      // thus work on tile k + 1 while the consumers filter tile k.
+      // k + 1 once the consumers are done with tile k - 1: the copy and the
+      // tensor cores work on tile k + 1 while the consumers filter tile k.
       for (int64_t k = 0; ok && k < ntiles; ++k) {
         const int b = (int)(k % kTBuf), x = (int)(k & 1);
         ok = mbar_wait(&sm.full[b], (uint32_t)((k / kTBuf) & 1));
@@ -589,9 +595,9 @@ tc_filter_kernel(const float* __restrict__ XT, const unsigned char* __restrict__
                       p > 0 || ks > 0);
         umma_commit(&sm.mdone[x]);
         umma_commit(&sm.sfree[b]);
-        const int64_t kt = k + 2;
-        if (kt < ntiles) {
-          if (k >= 1) ok = mbar_wait(&sm.sfree[(k - 1) % kTBuf], (uint32_t)(((k - 1) / kTBuf) & 1));
+        const int64_t kt = k + kTBuf - 1;  // into the buffer tile k - 1 used
+        if (kt < ntiles && kt >= kTBuf) {
+          ok = mbar_wait(&sm.sfree[(k - 1) % kTBuf], (uint32_t)(((k - 1) / kTBuf) & 1));
           if (!ok) break;
           fence_proxy_async();
           issue(kt);
@@ -616,38 +622,32 @@ tc_filter_kernel(const float* __restrict__ XT, const unsigned char* __restrict__
         break;
       }
       tc_fence_after();
-      float sacc[kTC];
+      const int64_t c0 = k * kTC;
+      const float4* cadj4 = reinterpret_cast<const float4*>(sm.Bt[b] + 3 * kTMat);
+      const float tq = sm.tau[row];
+      const float T = q >= n ? -kInf : (tq >= FLT_MAX ? kInf : (tq + Tu * tq) + (kTcK * nq - nq));
+      // acceptance masks, 32 candidates (one TMEM load) at a time; the
+      // query's own column is removed in the verify step
+      uint32_t mw[4];
 #pragma unroll
-      for (int c0 = 0; c0 < kTC; c0 += 32) {
+      for (int w4 = 0; w4 < 4; ++w4) {
         float v[32];
-        tmem_ld32(tmem + ((uint32_t)(wid * 32) << 16) + (uint32_t)(x * kTC + c0), v);
+        tmem_ld32(tmem + ((uint32_t)(wid * 32) << 16) + (uint32_t)(x * kTC + 32 * w4), v);
+        uint32_t mm = 0;
 #pragma unroll
-        for (int j = 0; j < 32; ++j) sacc[c0 + j] = v[j];
+        for (int j4 = 0; j4 < 8; ++j4) {
+          const float4 c = cadj4[8 * w4 + j4];
+          mm |= (fmaf(-2.0f, v[4 * j4 + 0], c.x) < T ? 1u : 0u) << (4 * j4 + 0);
+          mm |= (fmaf(-2.0f, v[4 * j4 + 1], c.y) < T ? 1u : 0u) << (4 * j4 + 1);
+          mm |= (fmaf(-2.0f, v[4 * j4 + 2], c.z) < T ? 1u : 0u) << (4 * j4 + 2);
+          mm |= (fmaf(-2.0f, v[4 * j4 + 3], c.w) < T ? 1u : 0u) << (4 * j4 + 3);
+        }
+        mw[w4] = mm;
       }
       tc_fence_before();
       __syncwarp();
       if (lane == 0) mbar_arrive(&sm.tfree[x]);  // accumulator buffer x may be overwritten
-      const int64_t c0 = k * kTC;
-      const float4* cadj4 = reinterpret_cast<const float4*>(sm.Bt[b] + 2 * kTMat);
-      const float tq = sm.tau[row];
-      const float T = q >= n ? -kInf : (tq >= FLT_MAX ? kInf : (tq + Tu * tq) + (kTcK * nq - nq));
-      // acceptance mask of the 128 candidates (the query's own column is
-      // removed in the verify step)
-      uint32_t m0 = 0, m1 = 0, m2 = 0, m3 = 0;
-#pragma unroll
-      for (int j4 = 0; j4 < kTC / 4; ++j4) {
-        const float4 c = cadj4[j4];
-        const float ca[4] = {c.x, c.y, c.z, c.w};
-#pragma unroll
-        for (int e = 0; e < 4; ++e) {
-          const int j = 4 * j4 + e;
-          const uint32_t bit = fmaf(-2.0f, sacc[j], ca[e]) < T ? 1u : 0u;
-          if (j < 32) m0 |= bit << j;
-          else if (j < 64) m1 |= bit << (j - 32);
-          else if (j < 96) m2 |= bit << (j - 64);
-          else m3 |= bit << (j - 96);
-        }
-      }
+      uint32_t m0 = mw[0], m1 = mw[1], m2 = mw[2], m3 = mw[3];
       // drain the masks in rounds of at most kTChunk pairs per lane
 #pragma unroll 1
       while (__any_sync(0xffffffffu, (m0 | m1 | m2 | m3) != 0)) {
@@ -676,11 +676,15 @@ tc_filter_kernel(const float* __restrict__ XT, const unsigned char* __restrict__
           const unsigned pr = sm.queue[wid][e];
           const int r = wid * 32 + (int)(pr >> 16), c = (int)(pr & 0xffffu);
           if (c0 + c == qbase + r) continue;  // the query itself
-          const float* cx = XT + k * 32 * kFC + c;
+          const unsigned char* tb = sm.Bt[b];
           float dd = 0.f;
 #pragma unroll
           for (int t = 0; t < kTDim; ++t) {
-            const float df = sm.qT[t][r] - __ldg(cx + t * kFC);
+            const uint32_t o = tc_off(c, t);
+            const float cv = (__bfloat162float(*reinterpret_cast<const __nv_bfloat16*>(tb + o)) +
+                              __bfloat162float(*reinterpret_cast<const __nv_bfloat16*>(tb + kTMat + o))) +
+                             __bfloat162float(*reinterpret_cast<const __nv_bfloat16*>(tb + 2 * kTMat + o));
+            const float df = sm.qT[t][r] - cv;
             dd = fmaf(df, df, dd);
           }
           if (dd < sm.tau[r]) {
