@@ -257,6 +257,45 @@ def measure_stages(args, dev, ev, U):
     return out
 
 
+def e2e_breakdown(snap, ad, args, dev):
+    """One more (untimed) tl.spectral call with a device synchronisation
+    around each stage: host->device copy, operator set-up, eigensolve and
+    the rest (device->host copy, weighting, writes)."""
+    import torch
+    from snapatac2_gb300 import _eigen, tools
+    out = {}
+    saved = {}
+
+    def wrap(mod, name, key):
+        f = getattr(mod, name)
+        saved[(mod, name)] = f
+
+        def g(*a, **k):
+            torch.cuda.synchronize(dev)
+            t = time.perf_counter()
+            r = f(*a, **k)
+            torch.cuda.synchronize(dev)
+            out[key] = out.get(key, 0.0) + time.perf_counter() - t
+            return r
+        setattr(mod, name, g)
+
+    wrap(tools, "csr_to_device", "h2d")
+    wrap(_eigen, "build_operator", "operator")
+    wrap(_eigen, "eigsh_lm", "eigensolve")
+    try:
+        torch.cuda.synchronize(dev)
+        t = time.perf_counter()
+        snap.tl.spectral(ad, features=None, n_comps=args.ncomps, block=args.block)
+        torch.cuda.synchronize(dev)
+        total = time.perf_counter() - t
+    finally:
+        for (mod, name), f in saved.items():
+            setattr(mod, name, f)
+    out["rest"] = total - sum(out.values())
+    out["total"] = total
+    return out
+
+
 def gather_ceiling(csr, block, dev):
     """Time the row gathers of both SpMM passes alone (sg_gather_ceiling) over
     this matrix's own index streams: the floor of each pass for this access
@@ -390,7 +429,8 @@ def run_gpu(args):
             torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
             e2e_ms = float(t.item())
         e2e = {"value": n * world / (e2e_ms / 1e3), "unit": "cells/s", "ms_per_step": e2e_ms,
-               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": d2h}
+               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": d2h,
+               "breakdown_s": e2e_breakdown(snap, ad, args, dev)}
 
     # ---- FP64 GPU form and accuracy of the mixed result --------------------
     fp64 = accuracy = None

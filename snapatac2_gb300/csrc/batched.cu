@@ -59,10 +59,18 @@ bproj_partial(const int64_t* __restrict__ cta_r0, const int64_t* __restrict__ ct
     for (int q = 0; q < CPT; ++q) {
       const int p = threadIdx.x + q * 256;
       if (p < ncols) {
-        for (int i = 0; i < nr; ++i) {
-          const T qv = Q[(base + i) * ldq + p];
+        // several rows' loads in flight, then their FMAs in row order
+        constexpr int RU = B * CPT * (int)sizeof(T) >= 64 ? 2 : 8;
+        for (int i0 = 0; i0 < nr; i0 += RU) {
+          T qv[RU];
 #pragma unroll
-          for (int c = 0; c < B; ++c) acc[q][c] = fma(qv, ws[i][c], acc[q][c]);
+          for (int u = 0; u < RU; ++u) qv[u] = i0 + u < nr ? Q[(base + i0 + u) * ldq + p] : T(0);
+#pragma unroll
+          for (int u = 0; u < RU; ++u)
+            if (i0 + u < nr) {
+#pragma unroll
+              for (int c = 0; c < B; ++c) acc[q][c] = fma(qv[u], ws[i0 + u][c], acc[q][c]);
+            }
         }
       }
     }
@@ -106,22 +114,32 @@ bupdate_kernel(int64_t nrows, const int64_t* __restrict__ roff, int D, const int
     T acc[B];
 #pragma unroll
     for (int c = 0; c < B; ++c) acc[c] = T(0);
-    for (int p = lane; p < ncols; p += 32) {
-      const T qv = Q[i * ldq + p];
+    for (int p0 = 0; p0 < ncols; p0 += 8 * 32) {
+      T qv[8];
 #pragma unroll
-      for (int c = 0; c < B; ++c) acc[c] = fma(qv, (T)Cd[p * B + c], acc[c]);
+      for (int u = 0; u < 8; ++u) {
+        const int p = p0 + u * 32 + lane;
+        qv[u] = p < ncols ? Q[i * ldq + p] : T(0);
+      }
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int p = p0 + u * 32 + lane;
+        if (p < ncols) {
+#pragma unroll
+          for (int c = 0; c < B; ++c) acc[c] = fma(qv[u], (T)Cd[p * B + c], acc[c]);
+        }
+      }
     }
+    warp_colsum<T, B>(acc, lane);
+    int col = 0, live = B;
 #pragma unroll
-    for (int c = 0; c < B; ++c) {
-      T v = acc[c];
-#pragma unroll
-      for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-      acc[c] = v;
+    for (int o = 16; o >= 1; o >>= 1) {
+      if (live > 1) {
+        live /= 2;
+        if (lane & o) col += live;
+      }
     }
-    T mine = T(0);
-#pragma unroll
-    for (int c = 0; c < B; ++c) if (lane == c) mine = acc[c];
-    if (lane < B) W[i * B + lane] -= mine;
+    if ((lane % (32 / B)) == 0) W[i * B + col] -= acc[0];
   }
 }
 
@@ -129,6 +147,7 @@ bupdate_kernel(int64_t nrows, const int64_t* __restrict__ roff, int D, const int
 __global__ void bchol_kernel(int B, int D, const int* __restrict__ active, const double* __restrict__ G,
                              double* __restrict__ R, double* __restrict__ Rinv, int* status, int* bad_ds) {
   __shared__ double r[32][33];
+  __shared__ double x[32][33];  // x[i][j]: row i of column j of R^-1
   const int d = blockIdx.x;
   const int j = threadIdx.x;
   if (d >= D) return;
@@ -164,17 +183,17 @@ __global__ void bchol_kernel(int B, int D, const int* __restrict__ active, const
     atomicCAS(status, 0, SG_ERR_NUMERIC);
     if (bad_ds) atomicMin(bad_ds, d);
   }
+  // back substitution, lane j builds column j of R^-1 in shared memory
   if (j < B) {
-    double x[32];
-    for (int i = 0; i < 32; ++i) x[i] = 0.0;
-    x[j] = 1.0 / r[j][j];
+    for (int i = 0; i < B; ++i) x[i][j] = 0.0;
+    x[j][j] = 1.0 / r[j][j];
     for (int i = j - 1; i >= 0; --i) {
       double s = 0.0;
-      for (int t = i + 1; t <= j; ++t) s += r[i][t] * x[t];
-      x[i] = -s / r[i][i];
+      for (int t = i + 1; t <= j; ++t) s += r[i][t] * x[t][j];
+      x[i][j] = -s / r[i][i];
     }
     for (int i = 0; i < B; ++i) {
-      Ri[i * B + j] = i <= j ? x[i] : 0.0;
+      Ri[i * B + j] = i <= j ? x[i][j] : 0.0;
       Ro[i * B + j] = r[i][j];
     }
   }
@@ -190,6 +209,27 @@ brinv_kernel(int64_t nrows, const int64_t* __restrict__ roff, int D, const int* 
   const int lane = threadIdx.x & 31;
   const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  if (B <= 8) {  // thread per row: W[i,:] <- W[i,:] Rinv, column c over k = 0..c in order
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nrows;
+         i += (int64_t)gridDim.x * blockDim.x) {
+      const int d = find_ds(roff_s, D, i);
+      if (active && !active[d]) continue;
+      const double* ri = Rinv + (int64_t)d * B * B;
+      T w[B], o[B];
+#pragma unroll
+      for (int k = 0; k < B; ++k) w[k] = W[i * B + k];
+#pragma unroll
+      for (int c = 0; c < B; ++c) {
+        T s = T(0);
+#pragma unroll
+        for (int k = 0; k <= c; ++k) s = fma(w[k], (T)ri[k * B + c], s);
+        o[c] = s;
+      }
+#pragma unroll
+      for (int c = 0; c < B; ++c) W[i * B + c] = o[c];
+    }
+    return;
+  }
   for (int64_t i = gw; i < nrows; i += nw) {
     const int d = find_ds(roff_s, D, i);
     if (active && !active[d]) continue;
@@ -269,10 +309,15 @@ template <typename T, int B>
 int bproj_t(int ncta, const int64_t* r0, const int64_t* r1, const int* cta_ds, const int* active, const int* ds_cta,
             int D, const T* Q, int64_t ldq, int ncols, const T* W, double* part, double* C, int64_t cstride,
             cudaStream_t s) {
-  for (int c0 = 0; c0 < ncols; c0 += 512) {
-    const int nc = ncols - c0 < 512 ? ncols - c0 : 512;
-    if (nc <= 256) bproj_partial<T, B, 1><<<ncta, 256, 0, s>>>(r0, r1, cta_ds, active, Q + c0, ldq, nc, W, part);
-    else bproj_partial<T, B, 2><<<ncta, 256, 0, s>>>(r0, r1, cta_ds, active, Q + c0, ldq, nc, W, part);
+  constexpr int kSlice = B * (int)sizeof(T) >= 128 ? 256 : 512;  // two thread columns only while they fit
+  for (int c0 = 0; c0 < ncols; c0 += kSlice) {
+    const int nc = ncols - c0 < kSlice ? ncols - c0 : kSlice;
+    if constexpr (kSlice > 256) {
+      if (nc > 256) bproj_partial<T, B, 2><<<ncta, 256, 0, s>>>(r0, r1, cta_ds, active, Q + c0, ldq, nc, W, part);
+      else bproj_partial<T, B, 1><<<ncta, 256, 0, s>>>(r0, r1, cta_ds, active, Q + c0, ldq, nc, W, part);
+    } else {
+      bproj_partial<T, B, 1><<<ncta, 256, 0, s>>>(r0, r1, cta_ds, active, Q + c0, ldq, nc, W, part);
+    }
     SG_CHECK_LAUNCH();
     const int tot = nc * B;
     dim3 g((tot + 255) / 256, D);

@@ -47,6 +47,34 @@ template <> struct V16<double> {
   }
 };
 
+// Column sums of a B-wide row block held as per-lane partials acc[0..B-1]:
+// a transpose butterfly (lane pairs swap half of their sums at each step)
+// leaves column c's total in acc[0] of the 32/B lanes whose high bits spell
+// c, after B - 1 + 5 - log2(B) shuffles.  Fixed order: deterministic.
+template <typename T, int B>
+__device__ __forceinline__ void warp_colsum(T (&acc)[B], int lane) {
+  // halve the columns a lane holds while doubling the lanes each sum covers
+  int live = B;
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) {
+    if (live > 1) {
+      const int half = live / 2;
+      const bool upper = (lane & o) != 0;
+#pragma unroll
+      for (int c = 0; c < B / 2; ++c) {
+        if (c < half) {
+          const T send = upper ? acc[c] : acc[c + half];
+          const T recv = __shfl_xor_sync(0xffffffffu, send, o);
+          acc[c] = (upper ? acc[c + half] : acc[c]) + recv;
+        }
+      }
+      live = half;
+    } else {
+      acc[0] += __shfl_xor_sync(0xffffffffu, acc[0], o);
+    }
+  }
+}
+
 // ---- mbarrier + bulk asynchronous copy (cp.async.bulk) helpers -----------
 constexpr uint64_t kWaitNs = 2000000000ull;  // bounded mbarrier wait: 2 s
 

@@ -169,30 +169,6 @@ proj_reduce(int nparts, int ncols, int B, const double* __restrict__ part, doubl
 // the 32/B lanes whose high bits spell its index, with B - 1 + 5 - log2(B)
 // shuffles instead of 5 B.  Fixed order: deterministic.
 template <typename T, int B>
-__device__ __forceinline__ void warp_colsum(T (&acc)[B], int lane) {
-  // halve the columns a lane holds while doubling the lanes each sum covers
-  int live = B;
-#pragma unroll
-  for (int o = 16; o >= 1; o >>= 1) {
-    if (live > 1) {
-      const int half = live / 2;
-      const bool upper = (lane & o) != 0;
-#pragma unroll
-      for (int c = 0; c < B / 2; ++c) {
-        if (c < half) {
-          const T send = upper ? acc[c] : acc[c + half];
-          const T recv = __shfl_xor_sync(0xffffffffu, send, o);
-          acc[c] = (upper ? acc[c + half] : acc[c]) + recv;
-        }
-      }
-      live = half;
-    } else {
-      acc[0] += __shfl_xor_sync(0xffffffffu, acc[0], o);
-    }
-  }
-}
-
-template <typename T, int B>
 __global__ void __launch_bounds__(256)
 update_kernel(int64_t n, const T* __restrict__ Q, int64_t ldq, int ncols, const double* __restrict__ C,
               T* __restrict__ W) {
@@ -418,11 +394,18 @@ __global__ void fill_random(int64_t count, uint64_t seed, T* __restrict__ out) {
 template <typename T, int B>
 int proj_t(int64_t n, const T* Q, int64_t ldq, int ncols, const T* W, double* part, int nparts, double* C,
            cudaStream_t s) {
-  // column slices of at most 2 * kProjBlock basis vectors per launch
-  for (int c0 = 0; c0 < ncols; c0 += 2 * kProjBlock) {
-    const int nc = ncols - c0 < 2 * kProjBlock ? ncols - c0 : 2 * kProjBlock;
-    if (nc <= kProjBlock) proj_partial<T, B, 1><<<nparts, kProjBlock, 0, s>>>(n, Q + c0, ldq, nc, W, part);
-    else proj_partial<T, B, 2><<<nparts, kProjBlock, 0, s>>>(n, Q + c0, ldq, nc, W, part);
+  // column slices of at most 2 * kProjBlock basis vectors per launch (one
+  // slice per thread column when a row of W is 128 bytes or more: two would
+  // not fit the register file)
+  constexpr int kSlice = (B * (int)sizeof(T) >= 128 ? 1 : 2) * kProjBlock;
+  for (int c0 = 0; c0 < ncols; c0 += kSlice) {
+    const int nc = ncols - c0 < kSlice ? ncols - c0 : kSlice;
+    if constexpr (kSlice > kProjBlock) {
+      if (nc > kProjBlock) proj_partial<T, B, 2><<<nparts, kProjBlock, 0, s>>>(n, Q + c0, ldq, nc, W, part);
+      else proj_partial<T, B, 1><<<nparts, kProjBlock, 0, s>>>(n, Q + c0, ldq, nc, W, part);
+    } else {
+      proj_partial<T, B, 1><<<nparts, kProjBlock, 0, s>>>(n, Q + c0, ldq, nc, W, part);
+    }
     SG_CHECK_LAUNCH();
     const int tot = nc * B;
     proj_reduce<<<(tot + 31) / 32, kReduceWarps * 32, 0, s>>>(nparts, nc, B, part, C + (int64_t)c0 * B);
