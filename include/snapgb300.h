@@ -34,6 +34,10 @@ extern "C" {
 #define SG_ERR_CUDA 4     /* a CUDA launch or runtime call failed */
 #define SG_ERR_NUMERIC 5  /* numerical breakdown (e.g. non-positive Gram pivot) */
 #define SG_ERR_TIMEOUT 6  /* a bounded device-side wait gave up (copy never completed) */
+#define SG_ERR_PARSE 7    /* malformed fragment record, or a fragment without a barcode */
+#define SG_ERR_UNSORTED 8 /* sorted_by_barcode, but a barcode's records are not one run */
+#define SG_ERR_CONVERT 9  /* fragment size does not fit the matrix value type (u32 / i32) */
+#define SG_ERR_COLLISION 10 /* barcode hashes still collided after re-hashing (never seen) */
 
 /* Counting strategies, same meaning as CountingStrategy in
  * snapatac2-core/src/feature_count/counter.rs:19-36 ("insertion", "fragment",
@@ -102,6 +106,72 @@ int sg_tile_emit(int64_t n_cells, const int64_t* key_ptr, const void* scratch,
                  int64_t scratch_bytes, const int64_t* out_indptr, int32_t* out_idx,
                  uint32_t* out_cnt, int64_t cap, int* status, void* stream);
 
+
+/* ------------------------------------------------------------------------ */
+/* Fragment-file import -- replaces the PyO3 import_fragments               */
+/*   (snapatac2-python/src/preprocessing.rs:87-184) and                     */
+/*   snapatac2-core/src/preprocessing/import.rs:31-210 (grouping by barcode, */
+/*   QC, per-cell sort) with the record syntax of qc.rs:303-348.  The file   */
+/*   itself (gzip / plain) is read and decompressed by the caller; `text` is */
+/*   its bytes in device memory (16-byte aligned).                           */
+/*                                                                           */
+/*   1. sg_frag_count_lines  -> number of lines (synchronises the stream)    */
+/*   2. sg_frag_index_lines  -> line_start[n_lines + 1]                      */
+/*   3. sg_frag_import       -> everything in `workspace`; sizes in info     */
+/*   4. sg_frag_emit         -> copies the results into exact-size arrays    */
+/* ------------------------------------------------------------------------ */
+
+/* Bytes of scratch for sg_frag_count_lines / sg_frag_index_lines.          */
+int64_t sg_frag_line_scratch_bytes(int64_t nbytes);
+/* *n_lines (host) = number of '\n' plus one for an unterminated last line. */
+int sg_frag_count_lines(const uint8_t* text, int64_t nbytes, void* scratch, int64_t* n_lines, void* stream);
+/* line_start[i] = first byte of line i; line_start[n_lines] = nbytes, or   */
+/* nbytes + 1 when the last line has no newline.  Same scratch as above.    */
+int sg_frag_index_lines(const uint8_t* text, int64_t nbytes, const void* scratch, int64_t n_lines,
+                        int64_t* line_start, void* stream);
+
+/* Bytes of workspace for sg_frag_import / sg_frag_emit (about 300 B per    */
+/* line plus 32 B per whitelist entry).                                      */
+int64_t sg_frag_workspace_bytes(int64_t n_lines, int64_t n_whitelist);
+
+/* The import.  Chromosomes: n_chrom names sorted by bytes (chrom_blob +    */
+/* chrom_off[n_chrom + 1]), their lengths, the cumulative length before each */
+/* (chrom_base) and a mitochondrial flag per name; genome_size = total.      */
+/* Whitelist (has_whitelist != 0): n_whitelist byte strings (wl_blob +       */
+/* wl_off[n_whitelist + 1]).  min_num_fragments, sorted_by_barcode,          */
+/* shift_left, shift_right as in the reference; seed: barcode hash seed.     */
+/* info (host, 10 entries): [0] cells, [1] matrix entries, [2] paired (1),   */
+/* single-end (0) or no record (-1), [3] line of the first error or -1,      */
+/* [4] records with a barcode, [5] distinct barcodes, [6] re-hashes,         */
+/* [7] matrix sort path (0 = one 64-bit key, 1 = three keys), [8] kernels    */
+/* launched, [9] reserved.  Synchronous:                                     */
+/* returns after the stream has finished.  Errors: SG_ERR_PARSE (malformed   */
+/* line, or a fragment without a barcode), SG_ERR_UNSORTED, SG_ERR_RANGE     */
+/* (position past its chromosome), SG_ERR_CONVERT; info[3] names the line.   */
+int sg_frag_import(const uint8_t* text, int64_t nbytes, const int64_t* line_start, int64_t n_lines,
+                   const uint8_t* chrom_blob, const int64_t* chrom_off, const uint64_t* chrom_size,
+                   const uint64_t* chrom_base, const uint8_t* chrom_mito, int n_chrom, uint64_t genome_size,
+                   const uint8_t* wl_blob, const int64_t* wl_off, int64_t n_whitelist, int has_whitelist,
+                   uint64_t min_num_fragments, int sorted_by_barcode, int64_t shift_left, int64_t shift_right,
+                   uint64_t seed, void* workspace, int64_t workspace_bytes, int64_t* info, void* stream);
+
+/* Results of sg_frag_import (same n_lines, n_whitelist and info):         */
+/* out_indptr[cells + 1], out_indices[entries] (global base index),         */
+/* out_data[entries] (uint32 size for paired data, int32 signed size for    */
+/* single-end data), and per cell: barcode location in `text` (byte offset  */
+/* << 16 | length), n_fragment, frac_dup, frac_mito (qc.rs:454-465).        */
+int sg_frag_emit(const void* workspace, int64_t n_lines, int64_t n_whitelist, const int64_t* info,
+                 int64_t* out_indptr, int64_t* out_indices, int32_t* out_data, uint64_t* out_bc_loc,
+                 uint64_t* out_n_fragment, double* out_frac_dup, double* out_frac_mito, void* stream);
+
+/* Stable LSD radix sort of n uint64 keys (and uint64 payloads when vals is */
+/* not NULL) by key bits [begin_bit, end_bit), 8 bits per pass, between the */
+/* buffers (keys, vals) and (keys_alt, vals_alt); *result_in_alt (host) = 1 */
+/* when the result ended in the _alt buffers.  Used by the import; exported */
+/* for tests.  No reference counterpart (the reference sorts on the host).  */
+int64_t sg_radix_scratch_bytes(int64_t n);
+int sg_radix_sort_u64(int64_t n, uint64_t* keys, uint64_t* vals, uint64_t* keys_alt, uint64_t* vals_alt,
+                      int begin_bit, int end_bit, void* scratch, int* result_in_alt, void* stream);
 
 /* ------------------------------------------------------------------------ */
 /* Feature selection -- the `count` vector of select_features              */

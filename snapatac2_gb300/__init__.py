@@ -3,6 +3,8 @@
 Drop-in API (same names, keywords, defaults and output slots as
 ``snapatac2.pp`` / ``snapatac2.tl``):
 
+* ``pp.import_fragments`` -- fragment file -> per-cell fragment matrix + QC
+                             (parse, group by barcode, sort: GPU)
 * ``pp.add_tile_matrix``  -- fragments -> cell x 500 bp tile counts (GPU)
 * ``pp.select_features``  -- most accessible tiles (column counts on the GPU,
                              ranking on the host with NumPy's tie order)
@@ -31,8 +33,10 @@ def __getattr__(name):
     if name == "pp":
         from . import preprocessing as _p
         from . import _knn_api as _k
-        ns = _Namespace(add_tile_matrix=_p.add_tile_matrix, select_features=_p.select_features,
-                        knn=_k.knn, fragments_to_anndata=_p.fragments_to_anndata)
+        from . import _import as _i
+        ns = _Namespace(import_fragments=_i.import_fragments, add_tile_matrix=_p.add_tile_matrix,
+                        select_features=_p.select_features, knn=_k.knn,
+                        fragments_to_anndata=_p.fragments_to_anndata)
         globals()["pp"] = ns
         return ns
     if name == "tl":

@@ -23,6 +23,10 @@ SG_ERR_CAP = 3
 SG_ERR_CUDA = 4
 SG_ERR_NUMERIC = 5
 SG_ERR_TIMEOUT = 6
+SG_ERR_PARSE = 7
+SG_ERR_UNSORTED = 8
+SG_ERR_CONVERT = 9
+SG_ERR_COLLISION = 10
 
 _P = ctypes.c_void_p
 _I64 = ctypes.c_int64
@@ -42,6 +46,15 @@ SIGNATURES: dict[str, tuple] = {
                            _I64, _P, _P, _P, _P, _P]),
     "sg_tile_emit": (_I32, [_I64, _P, _P, _I64, _P, _P, _P, _I64, _P, _P]),
     "sg_col_counts": (_I32, [_I64, _I64, _P, _P, _P, _P, _P, _P, _P, _P]),
+    "sg_frag_line_scratch_bytes": (_I64, [_I64]),
+    "sg_frag_count_lines": (_I32, [_P, _I64, _P, _P, _P]),
+    "sg_frag_index_lines": (_I32, [_P, _I64, _P, _I64, _P, _P]),
+    "sg_frag_workspace_bytes": (_I64, [_I64, _I64]),
+    "sg_frag_import": (_I32, [_P, _I64, _P, _I64, _P, _P, _P, _P, _P, _I32, ctypes.c_uint64, _P, _P, _I64, _I32,
+                              ctypes.c_uint64, _I32, _I64, _I64, ctypes.c_uint64, _P, _I64, _P, _P]),
+    "sg_frag_emit": (_I32, [_P, _I64, _I64, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
+    "sg_radix_scratch_bytes": (_I64, [_I64]),
+    "sg_radix_sort_u64": (_I32, [_I64, _P, _P, _P, _P, _I32, _I32, _P, _P, _P]),
     "sg_csr_select_cols": (_I32, [_I64, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
     "sg_transpose_blocks": (_I32, []),
     "sg_transpose_work_bytes": (_I64, [_I64, _I64, _I32]),
@@ -95,6 +108,7 @@ KERNELS_PER_CALL = {
     "sg_bbasis_rotate": 1, "sg_bidf": 3, "sg_bmask": 1,
     "sg_adjoint_stage1": 1, "sg_adjoint_stage2": 1, "sg_adjoint_stage3": 1, "sg_adjoint_final": 1,
     "sg_square_values": 1,
+    "sg_frag_count_lines": 4, "sg_frag_index_lines": 1,
 }
 
 _lock = threading.Lock()

@@ -12,6 +12,10 @@ extern "C" const char* sg_status_string(int status) {
     case SG_ERR_CUDA: return "CUDA error";
     case SG_ERR_NUMERIC: return "numerical breakdown";
     case SG_ERR_TIMEOUT: return "device-side wait timed out";
+    case SG_ERR_PARSE: return "malformed fragment record";
+    case SG_ERR_UNSORTED: return "Please sort fragment file by barcodes";
+    case SG_ERR_CONVERT: return "fragment size does not fit the matrix value type";
+    case SG_ERR_COLLISION: return "barcode hash collision";
     default: return "unknown status";
   }
 }

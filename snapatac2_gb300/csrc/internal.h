@@ -14,6 +14,14 @@ constexpr int64_t kScanTile = (int64_t)kScanBlock * kScanItems;
 cudaError_t inclusive_scan_i64(int64_t* data, int64_t n, void* scratch, cudaStream_t s);
 int64_t scan_scratch_bytes(int64_t n);
 
+// Stable LSD radix sort of n 64-bit keys (and 64-bit payloads when vals is
+// not null) by key bits [begin_bit, end_bit), 8 bits per pass, ping-ponging
+// between (keys, vals) and (keys_alt, vals_alt); *in_alt tells which pair
+// holds the result.  `scratch` needs radix_scratch_bytes(n) bytes.
+cudaError_t radix_sort_u64(int64_t n, uint64_t* keys, uint64_t* vals, uint64_t* keys_alt, uint64_t* vals_alt,
+                           int begin_bit, int end_bit, void* scratch, cudaStream_t s, bool* in_alt);
+int64_t radix_scratch_bytes(int64_t n);
+
 inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 
 inline int grid_for(int64_t n, int block, int max_blocks = 1 << 20) {

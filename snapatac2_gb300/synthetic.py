@@ -281,3 +281,144 @@ def binary_csr_device(
     indptr = torch.zeros(n_cells + 1, dtype=torch.int64, device=dev)
     torch.cumsum(row_nnz, 0, out=indptr[1:])
     return indptr, torch.cat(parts), clusters
+
+
+# ---- fragment files ----------------------------------------------------------
+
+MITO_NAME, MITO_SIZE = "chrM", 16_569
+
+
+def cell_barcodes(n_cells: int, seed: int = 0) -> list[str]:
+    """Distinct 10x-style barcodes: 16 random bases + "-1"."""
+    rng = np.random.Generator(np.random.PCG64(seed + 7919))
+    out: list[str] = []
+    seen: set = set()
+    while len(out) < n_cells:
+        for row in rng.integers(0, 4, (n_cells - len(out), 16)):
+            b = "".join("ACGT"[i] for i in row) + "-1"
+            if b not in seen:
+                seen.add(b)
+                out.append(b)
+    return out
+
+
+def fragment_text(frags: FragmentMatrix, genome: list[tuple[str, int]], *, seed: int = 0,
+                  order: str = "position", dup_frac: float = 0.15, mito_frac: float = 0.02,
+                  single_end: bool = False, header: bool = True, device=None):
+    """A fragment file (uint8 torch tensor of its text) for ``frags``.
+
+    Lines ``chrom\\tstart\\tend\\tbarcode\\tcount[\\tstrand]\\n`` in the format
+    of ``snapatac2-core/src/preprocessing/qc.rs:303-348``; chromosome-local
+    0-based starts, ``end = start + length``.  ``count`` is 1, or 2..5 for a
+    ``dup_frac`` share of the lines (PCR duplicates); about ``mito_frac`` of
+    each cell's lines are added on ``chrM`` (16,569 bp).  ``order``:
+    "position" (chromosome, start: how 10x pipelines write them),
+    "barcode" (barcode bytes, then position) or "shuffle".  Built with torch
+    on ``device`` (fixed-width rows, then the padding dropped), so that large
+    files can be drawn on the GPU.
+    """
+    import torch
+    dev = torch.device(device) if device is not None else torch.device("cpu")
+    g = torch.Generator(device="cpu").manual_seed(seed + 104729)
+    names = [n for n, _ in genome] + [MITO_NAME]
+    sizes = np.array([s for _, s in genome] + [MITO_SIZE], dtype=np.int64)
+    base_end = np.cumsum(sizes[:-1])
+    n = frags.n_cells
+    counts = np.diff(frags.indptr)
+    cell = torch.repeat_interleave(torch.arange(n), torch.from_numpy(counts)).to(dev)
+    gpos = torch.from_numpy(frags.pos.astype(np.int64)).to(dev)
+    length = torch.from_numpy(frags.length.astype(np.int64)).to(dev)
+    bend = torch.from_numpy(base_end).to(dev)
+    chrom = torch.searchsorted(bend, gpos, right=True)
+    start = gpos - torch.cat([torch.zeros(1, dtype=torch.int64, device=dev), bend])[chrom]
+    # mitochondrial fragments
+    n_m = np.random.Generator(np.random.PCG64(seed + 31)).poisson(mito_frac * np.maximum(counts, 1))
+    if n_m.sum():
+        mcell = torch.repeat_interleave(torch.arange(n), torch.from_numpy(n_m)).to(dev)
+        mlen = torch.randint(50, 500, (int(n_m.sum()),), generator=g).to(dev)
+        mstart = (torch.rand(int(n_m.sum()), generator=g).to(dev) * (MITO_SIZE - mlen)).long()
+        cell = torch.cat([cell, mcell])
+        chrom = torch.cat([chrom, torch.full_like(mcell, len(names) - 1)])
+        start = torch.cat([start, mstart])
+        length = torch.cat([length, mlen])
+    F = int(cell.numel())
+    cnt = torch.ones(F, dtype=torch.int64, device=dev)
+    dup = torch.rand(F, generator=g).to(dev) < dup_frac
+    cnt[dup] = torch.randint(2, 6, (int(dup.sum()),), generator=g).to(dev)
+    strand = (torch.rand(F, generator=g).to(dev) < 0.5) if single_end else None
+    bcs = cell_barcodes(n, seed)
+    if order == "position":
+        key = (chrom << 40) | (start << 8) | torch.clamp(length, max=255)
+        perm = torch.sort(key, stable=True).indices
+    elif order == "barcode":
+        rank = np.empty(n, dtype=np.int64)
+        rank[np.argsort(np.array([b.encode() for b in bcs], dtype=object), kind="stable")] = np.arange(n)
+        r = torch.from_numpy(rank).to(dev)[cell]
+        key = (chrom << 40) | (start << 8) | torch.clamp(length, max=255)
+        perm = torch.sort(key, stable=True).indices
+        perm = perm[torch.sort(r[perm], stable=True).indices]
+    elif order == "shuffle":
+        perm = torch.randperm(F, generator=g).to(dev)
+    else:
+        raise ValueError(order)
+    cell, chrom, start, length, cnt = cell[perm], chrom[perm], start[perm], length[perm], cnt[perm]
+    end = start + length
+    if strand is not None:
+        strand = strand[perm]
+
+    def table(strings):
+        w = max(len(s) for s in strings)
+        t = np.zeros((len(strings), w), dtype=np.uint8)
+        ln = np.zeros(len(strings), dtype=np.int64)
+        for i, s in enumerate(strings):
+            b = s.encode()
+            t[i, :len(b)] = np.frombuffer(b, dtype=np.uint8)
+            ln[i] = len(b)
+        return torch.from_numpy(t).to(dev), torch.from_numpy(ln).to(dev)
+
+    def digits(v, w=20):
+        nd = torch.ones_like(v)
+        p = torch.full_like(v, 10)
+        for _ in range(w - 1):
+            nd += (v >= p).long()
+            p = p * 10
+        d = torch.zeros((v.numel(), w), dtype=torch.uint8, device=dev)
+        x = v.clone()
+        for k in range(w - 1, -1, -1):
+            d[:, k] = (x % 10 + 48).to(torch.uint8)
+            x = x // 10
+        col = torch.arange(w, device=dev)
+        return d, col.unsqueeze(0) >= (w - nd).unsqueeze(1)
+
+    ct, cl = table(names)
+    bt, bl = table(bcs)
+    parts, masks = [], []
+    tab = torch.full((F, 1), 9, dtype=torch.uint8, device=dev)
+    ones = torch.ones((F, 1), dtype=torch.bool, device=dev)
+    parts.append(ct[chrom]); masks.append(torch.arange(ct.shape[1], device=dev).unsqueeze(0) < cl[chrom].unsqueeze(1))
+    for v, w in ((start, 11), (end, 11)):
+        parts += [tab]; masks += [ones]
+        d, m = digits(v, w)
+        parts.append(d); masks.append(m)
+    parts += [tab]; masks += [ones]
+    parts.append(bt[cell]); masks.append(torch.arange(bt.shape[1], device=dev).unsqueeze(0) < bl[cell].unsqueeze(1))
+    parts += [tab]; masks += [ones]
+    d, m = digits(cnt, 2)
+    parts.append(d); masks.append(m)
+    if strand is not None:
+        parts += [tab]; masks += [ones]
+        parts.append(torch.where(strand, 45, 43).to(torch.uint8).unsqueeze(1)); masks.append(ones)
+    parts.append(torch.full((F, 1), 10, dtype=torch.uint8, device=dev)); masks.append(ones)
+    body = torch.cat(parts, 1)[torch.cat(masks, 1)]
+    if header:
+        h = torch.from_numpy(np.frombuffer(b"# synthetic fragments\n# columns: chrom start end barcode count\n",
+                                           dtype=np.uint8).copy()).to(dev)
+        body = torch.cat([h, body])
+    return body
+
+
+def fragment_genome(genome: list[tuple[str, int]]) -> dict:
+    """chrom_sizes for importing ``fragment_text`` output (with chrM)."""
+    d = dict(genome)
+    d[MITO_NAME] = MITO_SIZE
+    return d
