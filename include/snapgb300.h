@@ -108,6 +108,42 @@ int sg_tile_emit(int64_t n_cells, const int64_t* key_ptr, const void* scratch,
 
 
 /* ------------------------------------------------------------------------ */
+/* Cell-by-region counts (peak matrix) -- replaces create_peak_matrix over   */
+/*   fragments (snapatac2-core/src/feature_count/matrix.rs:95-170) with     */
+/*   RegionCounter::insert_fragment (feature_count/counter.rs:117-146) and   */
+/*   the fragments of pair_to_fragments / single_to_fragments               */
+/*   (feature_count/data_iter.rs:27-117), entered from the PyO3             */
+/*   mk_peak_matrix (snapatac2-python/src/preprocessing.rs:370-430).         */
+/*                                                                           */
+/* Fragments as for sg_tile_plan (frag_len ignored, may be NULL, for        */
+/* SG_COUNT_SINGLE).  Regions per chromosome c: [region_ptr[c],             */
+/* region_ptr[c + 1]) sorted by start, chromosome coordinates, end          */
+/* exclusive, region_maxend = running maximum of the ends within the        */
+/* chromosome, region_id = feature index (< n_features).  A region counts   */
+/* a query when start < query end and end > query start.  Strategies:      */
+/* SG_COUNT_INSERTION (+1 per insertion per region), SG_COUNT_FRAGMENT      */
+/* (+1 per fragment per overlapping region), SG_COUNT_PIC (+1 per region    */
+/* hit by either insertion), SG_COUNT_SINGLE (single-end reads: +1 per      */
+/* region containing the read's position).  min_len / max_len: size bounds  */
+/* of paired fragments, -1 = none.  A position past the genome sets         */
+/* SG_ERR_RANGE.  Two calls, then sg_tile_emit with the same scratch        */
+/* (sg_tile_scratch_bytes(key_ptr[n_cells]) bytes): the pairs are (feature, */
+/* count), features strictly increasing per row.                            */
+/* ------------------------------------------------------------------------ */
+int sg_region_plan(const int64_t* cell_ptr, int64_t n_cells, int64_t n_frags, const uint64_t* frag_pos,
+                   const uint32_t* frag_len, const uint64_t* chrom_end, const uint8_t* chrom_excl, int n_chrom,
+                   const int64_t* region_ptr, const uint64_t* region_start, const uint64_t* region_end,
+                   const uint64_t* region_maxend, const uint32_t* region_id, int64_t n_features, int strategy,
+                   int64_t min_len, int64_t max_len, int64_t* key_ptr, void* scan_scratch, int* status,
+                   unsigned long long* bad, void* stream);
+int sg_region_run(const int64_t* cell_ptr, int64_t n_cells, int64_t n_frags, const uint64_t* frag_pos,
+                  const uint32_t* frag_len, const uint64_t* chrom_end, const uint8_t* chrom_excl, int n_chrom,
+                  const int64_t* region_ptr, const uint64_t* region_start, const uint64_t* region_end,
+                  const uint64_t* region_maxend, const uint32_t* region_id, int64_t n_features, int strategy,
+                  int64_t min_len, int64_t max_len, const int64_t* key_ptr, void* scratch, int64_t scratch_bytes,
+                  int64_t* out_indptr, void* scan_scratch, int* status, unsigned long long* bad, void* stream);
+
+/* ------------------------------------------------------------------------ */
 /* Fragment-file import -- replaces the PyO3 import_fragments               */
 /*   (snapatac2-python/src/preprocessing.rs:87-184) and                     */
 /*   snapatac2-core/src/preprocessing/import.rs:31-210 (grouping by barcode, */

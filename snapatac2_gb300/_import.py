@@ -218,19 +218,31 @@ def import_text(text: bytes | np.ndarray | torch.Tensor, chrom_sizes, *, min_num
     """Import fragment-file text (bytes on the host, or a uint8 tensor) and
     return host arrays.  ``host_text`` (the same bytes on the host) saves
     reading the kept cells' barcodes back from the device."""
+    from .tools import _UPLOADS, release_uploads
     dev = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+    borrowed: list = []
     if isinstance(text, torch.Tensor):
         if text.dtype != torch.uint8:
             raise ValueError("text must be uint8")
-        d_text = text.to(dev)
+        if text.is_cuda:
+            d_text = text.to(dev)
+        else:  # host text: into a pooled device buffer (no first-touch cost on reuse)
+            buf = _UPLOADS.take(dev, torch.uint8, text.numel())
+            borrowed.append(buf)
+            d_text = buf[:text.numel()]
+            d_text.copy_(text, non_blocking=text.is_pinned())
     else:
         if host_text is None and isinstance(text, (bytes, bytearray)):
             host_text = text
         d_text = upload_text(text, dev)
-    r = import_device(d_text, chrom_sizes, min_num_fragments=min_num_fragments,
-                      sorted_by_barcode=sorted_by_barcode, whitelist=whitelist, chrM=chrM,
-                      shift_left=shift_left, shift_right=shift_right)
-    return to_host(r, d_text, host_text)
+    try:
+        r = import_device(d_text, chrom_sizes, min_num_fragments=min_num_fragments,
+                          sorted_by_barcode=sorted_by_barcode, whitelist=whitelist, chrM=chrM,
+                          shift_left=shift_left, shift_right=shift_right)
+        return to_host(r, d_text, host_text)
+    finally:
+        del d_text
+        release_uploads(borrowed)
 
 
 def _gather_barcodes(d_text: torch.Tensor, offs: np.ndarray, lens: np.ndarray) -> bytes:

@@ -46,6 +46,10 @@ SIGNATURES: dict[str, tuple] = {
                            _I64, _P, _P, _P, _P, _P]),
     "sg_tile_emit": (_I32, [_I64, _P, _P, _I64, _P, _P, _P, _I64, _P, _P]),
     "sg_col_counts": (_I32, [_I64, _I64, _P, _P, _P, _P, _P, _P, _P, _P]),
+    "sg_region_plan": (_I32, [_P, _I64, _I64, _P, _P, _P, _P, _I32, _P, _P, _P, _P, _P, _I64, _I32, _I64, _I64,
+                              _P, _P, _P, _P, _P]),
+    "sg_region_run": (_I32, [_P, _I64, _I64, _P, _P, _P, _P, _I32, _P, _P, _P, _P, _P, _I64, _I32, _I64, _I64,
+                             _P, _P, _I64, _P, _P, _P, _P, _P]),
     "sg_frag_line_scratch_bytes": (_I64, [_I64]),
     "sg_frag_count_lines": (_I32, [_P, _I64, _P, _P, _P]),
     "sg_frag_index_lines": (_I32, [_P, _I64, _P, _I64, _P, _P]),
@@ -108,7 +112,7 @@ KERNELS_PER_CALL = {
     "sg_bbasis_rotate": 1, "sg_bidf": 3, "sg_bmask": 1,
     "sg_adjoint_stage1": 1, "sg_adjoint_stage2": 1, "sg_adjoint_stage3": 1, "sg_adjoint_final": 1,
     "sg_square_values": 1,
-    "sg_frag_count_lines": 4, "sg_frag_index_lines": 1,
+    "sg_frag_count_lines": 4, "sg_frag_index_lines": 1, "sg_region_plan": 4, "sg_region_run": 5,
 }
 
 _lock = threading.Lock()

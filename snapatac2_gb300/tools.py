@@ -8,6 +8,7 @@ and output slots ``uns['spectral_eigenvalue']`` (float64[k']) and
 """
 from __future__ import annotations
 
+import threading
 from typing import Literal
 
 import warnings
@@ -32,17 +33,60 @@ def _device(device=None) -> torch.device:
     return torch.device("cuda", torch.cuda.current_device())
 
 
-def csr_to_device(X, device) -> DeviceCSR:
+class _UploadPool:
+    """Device buffers reused from call to call for matrices copied in from
+    host memory.  A block the allocator has to map afresh pays a first-touch
+    cost on its first write (a 1.7 GB copy then took 70-100 ms instead of
+    8 ms); a buffer kept here is written at the copy engine's rate.  One
+    buffer per (device, dtype), grown on demand, lent for one call at a time
+    (a second concurrent call gets its own allocation)."""
+
+    def __init__(self):
+        self._free: dict = {}
+        self._lock = threading.Lock()
+
+    def take(self, device, dtype, numel: int) -> torch.Tensor:
+        with self._lock:
+            b = self._free.pop((device, dtype), None)
+        if b is None or b.numel() < numel:
+            b = torch.empty(max(numel, 1), dtype=dtype, device=device)
+        return b
+
+    def give(self, buf: torch.Tensor) -> None:
+        key = (buf.device, buf.dtype)
+        with self._lock:
+            cur = self._free.get(key)
+            if cur is None or cur.numel() < buf.numel():
+                self._free[key] = buf
+
+
+_UPLOADS = _UploadPool()
+
+
+def csr_to_device(X, device, borrowed: list | None = None) -> DeviceCSR:
     """The matrix as a DeviceCSR on ``device``.
 
     Accepts a scipy CSR matrix (values kept only when not all equal to 1) or
     a DeviceCSR whose tensors live on the host (pinned memory gives
-    asynchronous copies) or already on the device.
+    asynchronous copies) or already on the device.  With ``borrowed`` (a
+    list), host tensors are copied into pooled device buffers, which are
+    appended to the list and must be handed back with ``release_uploads``
+    once the call no longer uses the matrix.
     """
     if isinstance(X, DeviceCSR):
         if X.indptr.device == device:
             return X
-        mv = lambda t: None if t is None else t.to(device, non_blocking=True)  # noqa: E731
+
+        def mv(t):
+            if t is None:
+                return None
+            if borrowed is None:
+                return t.to(device, non_blocking=True)
+            buf = _UPLOADS.take(device, t.dtype, t.numel())
+            borrowed.append(buf)
+            dst = buf[:t.numel()].view(t.shape)
+            dst.copy_(t, non_blocking=True)
+            return dst
         return DeviceCSR(mv(X.indptr), mv(X.indices), mv(X.data), X.shape)
     X = sp.csr_matrix(X)
     if not X.has_sorted_indices:
@@ -60,6 +104,13 @@ def csr_to_device(X, device) -> DeviceCSR:
     return DeviceCSR(ip, ix, val, X.shape)
 
 
+def release_uploads(borrowed: list) -> None:
+    """Hand pooled upload buffers back (see ``csr_to_device``)."""
+    for b in borrowed:
+        _UPLOADS.give(b)
+    borrowed.clear()
+
+
 def spectral_embedding(X, features=None, n_comps: int = 30, random_state: int = 0, feature_weights=None, *,
                        precision: str = "mixed", block: int = 8, device=None, return_info: bool = False,
                        **solver_kw):
@@ -70,10 +121,15 @@ def spectral_embedding(X, features=None, n_comps: int = 30, random_state: int = 
     ``X`` is a scipy CSR matrix or a ``DeviceCSR`` already on the GPU.
     """
     dev = _device(device)
-    csr = csr_to_device(X, dev)
-    csr = _eigen.select_columns(csr, features)
-    op = _eigen.build_operator(csr, feature_weights)
-    res = _eigen.eigsh_lm(op, n_comps, precision=precision, block=block, seed=random_state, **solver_kw)
+    borrowed: list = []
+    try:
+        csr = csr_to_device(X, dev, borrowed)
+        csr = _eigen.select_columns(csr, features)
+        op = _eigen.build_operator(csr, feature_weights)
+        res = _eigen.eigsh_lm(op, n_comps, precision=precision, block=block, seed=random_state, **solver_kw)
+        del op, csr
+    finally:
+        release_uploads(borrowed)
     if not res.info["converged"]:
         warnings.warn(f"spectral embedding did not reach the requested accuracy "
                       f"(max residual {max(res.info['residuals']):.2e}, {res.info['restarts']} restarts)",

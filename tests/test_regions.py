@@ -1,0 +1,106 @@
+"""snap.pp.make_peak_matrix: the oracle on hand-made rows (CPU), the GPU
+region counter against the oracle (GPU), and a property that ties it to the
+tile matrix: with every genome tile given as a peak, the peak matrix is the
+tile matrix."""
+import gzip
+
+import numpy as np
+import pytest
+
+from oracle import regions as org
+
+NAMES = ["chr1", "chr2"]
+SIZES = [1000, 500]
+
+
+def test_oracle_strategies():
+    # one paired fragment chr1:[100, 300): insertions at 100 and 299
+    ptr, pos, ln = [0, 1], [100], [200]
+    peaks = ["chr1:50-150", "chr1:250-400", "chr1:0-1000", "chr1:150-250", "chr2:0-10", "chr1:50-150"]
+    ip, ix, dv, names = org.region_counts(ptr, pos, ln, NAMES, SIZES, peaks, strategy="insertion")
+    assert names == ["chr1:50-150", "chr1:250-400", "chr1:0-1000", "chr1:150-250", "chr2:0-10"]  # repeat dropped
+    assert dict(zip(ix.tolist(), dv.tolist())) == {0: 1, 1: 1, 2: 2}     # both insertions in 0-1000
+    _, ix, dv, _ = org.region_counts(ptr, pos, ln, NAMES, SIZES, peaks, strategy="paired-insertion")
+    assert dict(zip(ix.tolist(), dv.tolist())) == {0: 1, 1: 1, 2: 1}
+    _, ix, dv, _ = org.region_counts(ptr, pos, ln, NAMES, SIZES, peaks, strategy="fragment")
+    assert dict(zip(ix.tolist(), dv.tolist())) == {0: 1, 1: 1, 2: 1, 3: 1}
+    _, ix, dv, _ = org.region_counts(ptr, pos, ln, NAMES, SIZES, peaks, strategy="fragment", max_frag_size=150)
+    assert ix.size == 0
+    # single-end: the stored position only (1000 + 5 is chr2:5)
+    _, ix, dv, _ = org.region_counts([0, 2], [100, 1005], [10, -3], NAMES, SIZES, peaks, paired=False)
+    assert dict(zip(ix.tolist(), dv.tolist())) == {0: 1, 2: 1, 4: 1}
+
+
+def _data(n_cells=30, seed=0):
+    from snapatac2_gb300 import synthetic as S
+    g = S.make_genome(total=8_000_000, n_chrom=6)
+    fr = S.make_fragments(n_cells, g, median_frags=400, enriched_bins=500, seed=seed)
+    rng = np.random.default_rng(seed)
+    peaks = []
+    for c, size in g:
+        starts = np.sort(rng.integers(0, size - 2000, 300))
+        widths = rng.choice([1, 200, 500, 5000], 300)
+        peaks += [f"{c}:{s}-{min(s + w, size + 50)}" for s, w in zip(starts.tolist(), widths.tolist())]
+    peaks += peaks[:7] + ["chrUn:0-100", f"{g[0][0]}:10-10", f"{g[1][0]}:0-{g[1][1]}"]
+    rng.shuffle(peaks)
+    return g, fr, peaks
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("strategy,kw", [("insertion", {}), ("paired-insertion", {}), ("fragment", {}),
+                                         ("paired-insertion", dict(min_frag_size=50, max_frag_size=300)),
+                                         ("single", {})])
+def test_gpu_region_counts_match_oracle(strategy, kw):
+    import torch
+    from snapatac2_gb300 import _regions
+    from snapatac2_gb300.genome import ChromSizes
+    seed = {"insertion": 1, "paired-insertion": 2, "fragment": 3, "single": 4}[strategy] + 10 * len(kw)
+    g, fr, peaks = _data(seed=seed)
+    names, sizes = [c for c, _ in g], [s for _, s in g]
+    paired = strategy != "single"
+    length = fr.length.astype(np.int64) if paired else np.where(np.arange(fr.n_fragments) % 2, 1, -1) * 7
+    ref = org.region_counts(fr.indptr, fr.pos, length, names, sizes, peaks, strategy=strategy, paired=paired, **kw)
+    dev = torch.device("cuda")
+    regs = _regions.build_regions(peaks, names, dev)
+    t_len = torch.from_numpy(length.astype(np.int32)).to(dev)
+    res = _regions.region_matrix(torch.from_numpy(fr.indptr).to(dev), torch.from_numpy(fr.pos.view(np.int64)).to(dev),
+                                 t_len, ChromSizes(g), regs, strategy=strategy, **kw)
+    assert regs.names == ref[3]
+    np.testing.assert_array_equal(res.indptr.cpu().numpy(), ref[0])
+    np.testing.assert_array_equal(res.indices.cpu().numpy(), ref[1])
+    np.testing.assert_array_equal(res.data.cpu().numpy().view(np.uint32), ref[2])
+
+
+@pytest.mark.gpu
+def test_gpu_peaks_as_tiles_equal_tile_matrix():
+    import snapatac2_gb300 as snap
+    from snapatac2_gb300 import synthetic as S
+    g = S.make_genome(total=4_000_000, n_chrom=4)
+    fr = S.make_fragments(20, g, median_frags=300, enriched_bins=300, seed=3)
+    for strategy in ("insertion", "paired-insertion", "fragment"):
+        ad = snap.pp.fragments_to_anndata(fr.indptr, fr.pos, fr.length, g)
+        snap.pp.add_tile_matrix(ad, bin_size=500, exclude_chroms=None, counting_strategy=strategy)
+        peaks = list(ad.var_names)
+        pm = snap.pp.make_peak_matrix(ad, use_rep=peaks, counting_strategy=strategy)
+        assert list(pm.var_names) == peaks
+        assert (pm.X != ad.X).nnz == 0
+        assert pm.X.dtype == np.uint32
+
+
+@pytest.mark.gpu
+def test_gpu_make_peak_matrix_api(tmp_path):
+    import snapatac2_gb300 as snap
+    g, fr, peaks = _data(n_cells=12, seed=9)
+    ad = snap.pp.fragments_to_anndata(fr.indptr, fr.pos, fr.length, g, obs_names=[f"c{i}" for i in range(12)])
+    p = tmp_path / "peaks.txt.gz"
+    with gzip.open(p, "wt") as fh:
+        fh.write("\n".join(peaks) + "\n")
+    a = snap.pp.make_peak_matrix(ad, peak_file=str(p))
+    ad.uns["peaks"] = {"Peaks": np.array(peaks, dtype=object)}
+    b = snap.pp.make_peak_matrix(ad)
+    assert list(a.obs_names) == [f"c{i}" for i in range(12)]
+    assert (a.X != b.X).nnz == 0 and list(a.var_names) == list(b.var_names)
+    with pytest.raises(RuntimeError):
+        snap.pp.make_peak_matrix(ad, peak_file=str(p), use_rep="peaks")
+    assert snap.pp.make_peak_matrix(ad, inplace=True) is None
+    assert (ad.X != b.X).nnz == 0
