@@ -7,6 +7,7 @@ Drop-in API (same names, keywords, defaults and output slots as
                              (parse, group by barcode, sort: GPU)
 * ``pp.add_tile_matrix``  -- fragments -> cell x 500 bp tile counts (GPU)
 * ``pp.make_peak_matrix`` -- fragments -> cell x peak counts (GPU)
+* ``pp.make_gene_matrix`` -- fragments -> cell x gene activity (GPU counting)
 * ``pp.select_features``  -- most accessible tiles (column counts on the GPU,
                              ranking on the host with NumPy's tie order)
 * ``tl.spectral``         -- matrix-free cosine spectral embedding (GPU)
@@ -36,8 +37,10 @@ def __getattr__(name):
         from . import _knn_api as _k
         from . import _import as _i
         from . import _regions as _r
+        from . import _genes as _g
         ns = _Namespace(import_fragments=_i.import_fragments, add_tile_matrix=_p.add_tile_matrix,
-                        make_peak_matrix=_r.make_peak_matrix, select_features=_p.select_features, knn=_k.knn,
+                        make_peak_matrix=_r.make_peak_matrix, make_gene_matrix=_g.make_gene_matrix,
+                        select_features=_p.select_features, knn=_k.knn,
                         fragments_to_anndata=_p.fragments_to_anndata)
         globals()["pp"] = ns
         return ns
