@@ -1,0 +1,138 @@
+"""Nyström spectral embedding (``snap.tl.spectral(sample_size=...)``) on the GPU.
+
+Follows ``spectral_embedding_nystrom`` (``snapatac2-python/src/embedding.rs:61-131``)
+and ``nystrom`` (``embedding.rs:193-267``), then ``orthogonalize``
+(``snapatac2-python/python/snapatac2/tools/_embedding.py:397-413``):
+
+1. IDF weights over all cells; landmarks drawn uniformly, or with
+   probability proportional to 1 / (degree - 1) (``sample_method="degree"``,
+   ``compute_degrees`` / ``compute_probs``, ``embedding.rs:328-365``);
+2. the landmark rows, normalised with the global weights, embedded by the
+   same matrix-free eigensolver as the full path (``spectral_mf``);
+3. every cell extended out of sample with two FP64 SpMM launches
+   (W = seedᵀ · (u / sqrt(d) / λ) over the landmarks' CSC, q = X̂ · W over all
+   cells), each chunk of ``chunk_size`` rows rescaled by
+   sqrt(q · (Σ_chunk q ⊙ λ)) as the reference's per-chunk Python does;
+4. ``orthogonalize``: the singular values and right vectors of q from its
+   k x k Gram matrix, the k x k eigenproblem on the host, one n x k x k
+   product on the device.
+
+The reference draws its landmarks with ``rand::rngs::StdRng::seed_from_u64(2023)``
+(rand 0.8, third-party); this module draws them with NumPy's generator
+(same distributions: uniform, or successive weighted sampling without
+replacement), or takes them from ``landmarks=`` so that results can be
+compared for a given landmark set.
+"""
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from . import _eigen, _lib
+from ._binning import DeviceCSR
+
+
+def select_rows(csr: DeviceCSR, rows: torch.Tensor) -> DeviceCSR:
+    """The CSR rows ``rows`` (in that order), on the device."""
+    ip = csr.indptr
+    lens = (ip[1:] - ip[:-1])[rows]
+    ptr = torch.zeros(rows.numel() + 1, dtype=torch.int64, device=ip.device)
+    ptr[1:] = torch.cumsum(lens, 0)
+    total = int(ptr[-1].item())
+    src0 = torch.repeat_interleave(ip[:-1][rows], lens)
+    off = torch.arange(total, device=ip.device) - torch.repeat_interleave(ptr[:-1], lens)
+    pos = src0 + off
+    data = None if csr.data is None else csr.data[pos]
+    return DeviceCSR(ptr, csr.indices[pos].contiguous(), data, (int(rows.numel()), csr.shape[1]))
+
+
+def _spmm64(rows, ptr, idx, val, inp, out, scale, block, stream):
+    L = _lib.load()
+    _lib.check(L.sg_spmm(1, block, rows, ptr.data_ptr(), idx.data_ptr(), None if val is None else val.data_ptr(),
+                         inp.data_ptr(), out.data_ptr(), scale.data_ptr(), None, None, -1, stream), "sg_spmm (FP64)")
+
+
+def orthogonalize(evals: np.ndarray, q: torch.Tensor):
+    """``orthogonalize`` (``_embedding.py:397-413``): the eigenpairs of
+    diag(σ) Vᵀ diag(λ) V diag(σ) from the SVD q = U diag(σ) Vᵀ, mapped back
+    through q V diag(1/σ); returns (evals, n x k evecs on the device)."""
+    G = (q.T @ q).cpu().numpy()
+    lam, V = np.linalg.eigh(G)
+    order = np.argsort(lam)[::-1]
+    lam, V = lam[order], V[:, order]
+    sigma = np.sqrt(np.maximum(lam, 0.0))
+    B = np.multiply(V.T, evals.reshape((1, -1))) @ V
+    B *= sigma.reshape((-1, 1))
+    B *= sigma.reshape((1, -1))
+    evals_new, evecs_new = np.linalg.eig(B)
+    evals_new, evecs_new = np.real(evals_new), np.real(evecs_new)
+    ix = evals_new.argsort()[::-1]
+    evals_new, evecs_new = evals_new[ix], evecs_new[:, ix]
+    evecs_new = evecs_new / sigma.reshape((-1, 1))
+    M = torch.from_numpy(np.ascontiguousarray(V @ evecs_new)).to(q.device)
+    return evals_new, q @ M
+
+
+def spectral_nystrom(X, features=None, n_comps: int = 30, sample_size: int = 1000, *,
+                     weighted_by_degree: bool = False, chunk_size: int = 20000, feature_weights=None,
+                     landmarks=None, seed: int = 2023, random_state: int = 0, precision: str = "auto",
+                     block: int = 8, device=None, return_info: bool = False):
+    """(evals, evecs) of the Nyström embedding: evecs float64 (n, k), the
+    landmark eigenvalues re-estimated by ``orthogonalize``."""
+    from .tools import _device, csr_to_device, release_uploads
+    dev = _device(device)
+    borrowed: list = []
+    try:
+        csr = csr_to_device(X, dev, borrowed)
+        csr = _eigen.select_columns(csr, features)
+        n, m = csr.shape
+        op = _eigen.build_operator(csr, feature_weights)     # global IDF weights, row norms, degrees
+        if landmarks is None:
+            rng = np.random.default_rng(seed)
+            if weighted_by_degree:
+                inv = op.dinv.cpu().numpy()                   # 1 / (degree - 1)
+                landmarks = rng.choice(n, sample_size, replace=False, p=inv / inv.sum())
+            else:
+                landmarks = rng.choice(n, sample_size, replace=False)
+        lm = torch.as_tensor(np.asarray(landmarks, dtype=np.int64)).to(dev)
+        seed_csr = select_rows(csr, lm)
+        op_s = _eigen.build_operator(seed_csr, op.w)          # landmarks with the global weights
+        if precision == "auto":
+            from .tools import AUTO_FP64_CELLS
+            precision = "fp64" if op_s.n < AUTO_FP64_CELLS else "mixed"
+        res = _eigen.eigsh_lm(op_s, n_comps, precision=precision, block=block, seed=random_state)
+        v = np.asarray(res.evals, dtype=np.float64)
+        k = v.size
+        sh = torch.cuda.current_stream(dev).cuda_stream
+        f64 = dict(dtype=torch.float64, device=dev)
+        q = torch.empty(n, k, **f64)
+        # evecs / sqrt(d) / λ with d = degree - 1 of the landmark graph, then seedᵀ (·) and X̂ (·), 32 columns a launch
+        ev = res.evecs * op_s.dinv.sqrt().unsqueeze(1) / torch.from_numpy(v).to(dev).unsqueeze(0)
+        for c0 in range(0, k, 32):
+            kc = min(32, k - c0)
+            blk = 32 if kc > 16 else (16 if kc > 8 else (8 if kc > 4 else 4))
+            inp = torch.zeros(op_s.n, blk, **f64)
+            inp[:, :kc] = ev[:, c0:c0 + kc] * op_s.rinv.unsqueeze(1)
+            W = torch.empty(m, blk, **f64)
+            _spmm64(m, op_s.colptr, op_s.rowidx, op_s.cvalues, inp, W, op.w, blk, sh)
+            W *= op.w.unsqueeze(1)
+            Q = torch.empty(n, blk, **f64)
+            _spmm64(n, csr.indptr, csr.indices, csr.data, W, Q, op.rinv, blk, sh)
+            q[:, c0:c0 + kc] = Q[:, :kc]
+        vt = torch.from_numpy(v).to(dev)
+        for r0 in range(0, n, chunk_size):
+            qc = q[r0:r0 + chunk_size]
+            t = qc.sum(0) * vt
+            d = qc @ t
+            pos = d > 0
+            if bool((~pos).any()):
+                d = torch.where(pos, d, d[pos].min())
+            qc /= d.sqrt().unsqueeze(1)
+        evals, evecs = orthogonalize(v, q)
+        info = {"landmarks": int(lm.numel()), "landmark_solve": res.info}
+        del op, op_s, csr, seed_csr
+    finally:
+        release_uploads(borrowed)
+    if return_info:
+        return evals, evecs, info
+    return evals, evecs.cpu().numpy()

@@ -156,7 +156,8 @@ def spectral(
     block: int = 8,
     device=None,
 ):
-    """Laplacian-eigenmap embedding (``_embedding.py:129-295``), cosine, full sample.
+    """Laplacian-eigenmap embedding (``_embedding.py:129-295``), cosine; the full
+    sample, or the Nyström extension from ``sample_size`` landmarks.
 
     Extra keywords: ``precision`` ('mixed': FP32 SpMM and basis, FP64
     Rayleigh-Ritz and a final FP64 correction sweep; 'fp64': all FP64;
@@ -183,15 +184,20 @@ def spectral(
         if sample_size <= 0.0 or sample_size > 1.0:
             raise ValueError("when sample_size is a float, it should be > 0 and <= 1")
         sample_size = int(sample_size * n_sample)
-    if sample_size < n_sample:
-        raise NotImplementedError("Nyström sampling (sample_size < n_obs) is not supported")
     if distance_metric != "cosine":
         raise NotImplementedError("only distance_metric='cosine' (matrix-free) is supported")
-
-    if precision == "auto":
-        precision = "fp64" if adata.n_obs < AUTO_FP64_CELLS else "mixed"
-    evals, evecs = spectral_embedding(adata.X, features, n_comps, random_state, feature_weights,
-                                      precision=precision, block=block, device=device)
+    if sample_size < n_sample:
+        # Nyström (embedding.rs:61-131): landmark solve with random_state 0, as the reference
+        from ._nystrom import spectral_nystrom
+        evals, evecs = spectral_nystrom(adata.X, features, n_comps, sample_size,
+                                        weighted_by_degree=sample_method != "random", chunk_size=chunk_size,
+                                        feature_weights=feature_weights, random_state=0, precision=precision,
+                                        block=block, device=device)
+    else:
+        if precision == "auto":
+            precision = "fp64" if adata.n_obs < AUTO_FP64_CELLS else "mixed"
+        evals, evecs = spectral_embedding(adata.X, features, n_comps, random_state, feature_weights,
+                                          precision=precision, block=block, device=device)
     if weighted_by_sd:
         idx = [i for i in range(evals.shape[0]) if evals[i] > 0]
         evals = evals[idx]
