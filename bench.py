@@ -419,11 +419,9 @@ def run_gpu(args):
     spmm_ev = _eigen.SPMM_EVENTS
     _eigen.SPMM_EVENTS = None
     launches = counter.count
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = n * world / (ms / 1e3)
+    from snapatac2_gb300._replicas import replica_throughput
+    cells_all, ms = replica_throughput(n, ms, dev)
+    value = cells_all / (ms / 1e3)
 
     # SpMM roofline (dominant kernel), from the events of the timed region
     t_time = x_time = 0.0
@@ -475,11 +473,8 @@ def run_gpu(args):
         e2e_ms = (time.perf_counter() - t0) * 1e3 / args.e2e_steps
         e2e_step_ms = [round((b - a) * 1e3, 1) for a, b in zip([t0] + step_ends[:-1], step_ends)]
         d2h = int(ad.obsm["X_spectral"].size * 8 + ad.uns["spectral_eigenvalue"].size * 8)
-        if world > 1:
-            t = torch.tensor([e2e_ms], device=dev)
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            e2e_ms = float(t.item())
-        e2e = {"value": n * world / (e2e_ms / 1e3), "unit": "cells/s", "ms_per_step": e2e_ms,
+        cells_all, e2e_ms = replica_throughput(n, e2e_ms, dev)
+        e2e = {"value": cells_all / (e2e_ms / 1e3), "unit": "cells/s", "ms_per_step": e2e_ms,
                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": d2h,
                "allocator_retries": torch.cuda.memory_stats(dev).get("num_alloc_retries", 0) - retries0,
                "raw_indices_h2d_ms": {"before": raw_before, "after": raw_h2d(),
