@@ -71,6 +71,26 @@ def test_gradient_matches_dense_fp64_reference(valued, precision, rtol):
 
 
 @pytest.mark.gpu
+def test_gradient_matches_dense_fp64_reference_2k_cells():
+    """The dense FP64 reference gradient on a 2,000-cell subsample."""
+    import torch
+    from snapatac2_gb300._adjoint import topk_eigenvalue_sum
+    X, w = small_problem(False, n=2000, m=6000, seed=13)
+    Xd = torch.from_numpy(X.toarray())
+    wt = torch.from_numpy(w).requires_grad_(True)
+    _, lam = dense_topk_sum(wt.detach(), Xd, 40)
+    k = pick_k(np.sort(np.abs(lam.numpy()))[::-1])
+    f_ref, _ = dense_topk_sum(wt, Xd, k)
+    (g_ref,) = torch.autograd.grad(f_ref, wt)
+    wg = torch.from_numpy(w).cuda().requires_grad_(True)
+    f = topk_eigenvalue_sum(wg, X, k, precision="fp64", tol_vec=1e-12, tol_val=1e-12)
+    f.backward()
+    assert abs(float(f.detach()) - float(f_ref.detach())) <= 1e-5 * abs(float(f_ref.detach()))
+    g = wg.grad.cpu().numpy()
+    assert np.abs(g - g_ref.numpy()).max() / np.abs(g_ref.numpy()).max() <= 1e-6
+
+
+@pytest.mark.gpu
 def test_gradient_matches_central_differences():
     import torch
     from snapatac2_gb300._adjoint import topk_eigenvalue_sum
@@ -85,7 +105,7 @@ def test_gradient_matches_central_differences():
     g = wg.grad.cpu().numpy()
     rng = np.random.default_rng(0)
     eps = 1e-5
-    for _ in range(8):
+    for _ in range(64):  # 64 random unit directions
         v = rng.standard_normal(w.shape[0])
         v /= np.linalg.norm(v)
         fp = float(topk_eigenvalue_sum(torch.from_numpy(w + eps * v).cuda(), X, k, **kw))
