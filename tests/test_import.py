@@ -224,6 +224,25 @@ def test_gpu_import_file_api(tmp_path):
 
 
 @pytest.mark.gpu
+def test_gpu_import_device_text_and_plain_file(tmp_path):
+    """Text already on the device (barcodes read back from it) and a plain,
+    uncompressed file read straight into pinned memory."""
+    import torch
+    import snapatac2_gb300 as snap
+    from snapatac2_gb300 import _import
+    text, genome = _synthetic(n_cells=15, order="shuffle", seed=8)
+    kw = dict(sorted_by_barcode=False, min_num_fragments=20)
+    ref = ofr.import_fragments(text, genome, **kw)
+    d = torch.frombuffer(bytearray(text), dtype=torch.uint8).cuda()
+    _check_same(_import.import_text(d, genome, **kw), ref)
+    p = tmp_path / "frags.tsv"
+    p.write_bytes(text)
+    ad = snap.pp.import_fragments(str(p), genome, **kw)
+    assert list(ad.obs_names) == ref["obs_names"]
+    np.testing.assert_array_equal(ad.obsm["fragment_paired"].data, ref["data"])
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("n,bits", [(1, 64), (1000, 64), (5000, 13), (70000, 40), (300001, 64)])
 def test_gpu_radix_sort_stable(n, bits):
     import ctypes
