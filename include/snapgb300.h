@@ -291,6 +291,16 @@ int sg_spmm_masked(int dtype, int block, int64_t rows, const int64_t* ptr, const
                    const void* in, void* out, const void* scale, const void* dshift, const void* y, int grid,
                    int variant, const unsigned char* row_mask, void* stream);
 
+/* sg_spmm_masked on a persistent grid whose warps take 4 rows at a time    */
+/* from *counter (device, zeroed by this call on `stream`): rows of very     */
+/* different lengths leave no tail.  Same per-row arithmetic and result.     */
+/* FP32 only (dtype 0); variant as for sg_spmm_ex; rows < 2^31.  Calls that  */
+/* run concurrently need separate counters.  No reference counterpart (a    */
+/* schedule of the Gram matvec of embedding.rs:155-188).                    */
+int sg_spmm_dyn(int dtype, int block, int64_t rows, const int64_t* ptr, const int32_t* idx, const float* val,
+                const void* in, void* out, const void* scale, const void* dshift, const void* y, int variant,
+                const unsigned char* row_mask, unsigned int* counter, void* stream);
+
 /* Stage-tiled SpMM, same result contract as sg_spmm_masked (summation     */
 /* order differs at rounding level).  One CTA per SM (and wave) owns a row  */
 /* range; the dense operand `in` (cols x block, every row is read) streams  */

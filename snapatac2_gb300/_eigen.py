@@ -60,6 +60,7 @@ class GramOperator:
     variants: dict = field(default_factory=dict)  # (dtype, block) -> (Xᵀ pass, X pass)
     status: object = None  # DeviceStatus of the staged SpMM's bounded waits (created on first use)
     staged_tables: dict = field(default_factory=dict)  # (pass, row bytes) -> segment table (uint8)
+    counter: torch.Tensor | None = None  # row counters of the dynamically scheduled SpMM (one per pass)
 
     def scales(self, dtype_code: int):
         if dtype_code == 0:
@@ -86,7 +87,8 @@ class GramOperator:
         """One SpMM launch: which = 0 is T = w² ⊙ Xᵀ inp (CSC, rows = features),
         which = 1 is out = a ⊙ X inp - dinv ⊙ y (CSR, rows = cells).  Variants
         below STAGED select the gather kernel (sg_spmm_masked), STAGED + v
-        the stage-tiled kernel (sg_spmm_staged).  Returns the C status."""
+        the stage-tiled kernel (sg_spmm_staged), DYN + v the gather kernel
+        with dynamic row scheduling (sg_spmm_dyn).  Returns the C status."""
         L = _lib.load()
         w2, a, dinv = self.scales(dtype_code)
         if which == 0:
@@ -99,7 +101,13 @@ class GramOperator:
             val = self.csr.data.data_ptr() if self.csr.data is not None else None
             scale, dsh, yp = a.data_ptr(), dinv.data_ptr(), y.data_ptr()
             mask = self.row_mask.data_ptr() if self.row_mask is not None else None
-        if variant >= STAGED:
+        if variant >= DYN:
+            if self.counter is None:
+                self.counter = torch.zeros(2, dtype=torch.int32, device=self.a.device)
+            rc = L.sg_spmm_dyn(dtype_code, block, rows, ptr.data_ptr(), idx.data_ptr(), val, inp.data_ptr(),
+                               out.data_ptr(), scale, dsh, yp, variant - DYN, mask,
+                               self.counter.data_ptr() + 4 * which, stream)
+        elif variant >= STAGED:
             if self.status is None:
                 self.status = _lib.DeviceStatus(self.a.device)
             table = self.staged_table(which, dtype_code, block, stream)
@@ -138,8 +146,10 @@ class GramOperator:
 # solve is taken to sit at its FP32 noise floor (~ 2^-24 times a few hundred).
 FP32_FLOOR = 3e-5
 
-# Variant codes >= STAGED select the stage-tiled SpMM kernel.
+# Variant codes >= STAGED select the stage-tiled SpMM kernel, codes >= DYN the
+# gather kernel on a persistent grid with dynamic row chunks (FP32).
 STAGED = 100
+DYN = 200
 
 _TUNED: dict = {}
 
@@ -154,7 +164,8 @@ def tune_spmm(op: "GramOperator", code: int, block: int, Z, Zs, T, W, stream: in
     block buffers of the caller's shapes as operands.  The choice is cached
     per process for the shape class (dtype, block, n, m, nnz in units of
     2^20, valued, masked) and can be forced with
-    SNAPGB300_SPMM_VARIANT=<t>,<x> (codes >= 100 select the staged kernel).
+    SNAPGB300_SPMM_VARIANT=<t>,<x> (codes >= 100 select the staged kernel,
+    >= 200 the dynamically scheduled gather kernel).
     """
     import os
     forced = os.environ.get("SNAPGB300_SPMM_VARIANT")
@@ -171,6 +182,8 @@ def tune_spmm(op: "GramOperator", code: int, block: int, Z, Zs, T, W, stream: in
     if code == 1 and block > 8:  # FP64 wide blocks: the deeper unrolls spill
         gather = [v for v in gather if (v & 3) < 2]
     cands = gather + [STAGED + v for v in range(int(L.sg_spmm_staged_variants()))]
+    if code == 0:  # FP32: the same gathers on a persistent grid with dynamic row chunks
+        cands += [DYN + v for v in gather]
     # private operands: the caller's blocks hold live solver state
     Z, Zs, T, W = (torch.zeros_like(t) for t in (Z, Zs, T, W))
 

@@ -322,12 +322,18 @@ __device__ __forceinline__ VT gather16(const VT* p, bool l2only) {
   return l2only ? __ldcg(p) : __ldg(p);
 }
 
-template <typename T, int B, bool VALUED, bool SHIFT, int VAR>
+// DYN: a persistent grid whose warps take kDynRows rows at a time from an
+// atomic counter (zeroed by the host before the launch), so that the long
+// rows of a skewed matrix do not leave a tail of idle SMs; each row is still
+// summed by one warp in the same order (same result as the static schedule).
+constexpr int kDynRows = 4;
+
+template <typename T, int B, bool VALUED, bool SHIFT, int VAR, bool DYN = false>
 __global__ void __launch_bounds__(256)
 spmm_kernel(int64_t rows, const int64_t* __restrict__ ptr, const int32_t* __restrict__ idx,
             const float* __restrict__ val, const T* __restrict__ in, T* __restrict__ out,
             const T* __restrict__ scale, const T* __restrict__ dshift, const T* __restrict__ y,
-            const unsigned char* __restrict__ row_mask) {
+            const unsigned char* __restrict__ row_mask, unsigned int* __restrict__ counter = nullptr) {
   using VT = typename V16<T>::type;
   constexpr int VW = V16<T>::n;
   constexpr int LPN = B / VW;          // lanes per nonzero
@@ -340,9 +346,24 @@ spmm_kernel(int64_t rows, const int64_t* __restrict__ ptr, const int32_t* __rest
   const int sub = lane % LPN, slot = lane / LPN;
   const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t r = gw; r < rows; r += nw) {
-    if (row_mask && !row_mask[r]) continue;  // frozen row (warp-uniform)
-    const int64_t s = ptr[r], e = ptr[r + 1];
+  int64_t r = DYN ? 0 : gw, rend = DYN ? 0 : rows;
+  while (true) {
+    if (DYN) {
+      if (r >= rend) {  // next chunk of rows for this warp
+        unsigned int c0 = 0;
+        if (lane == 0) c0 = atomicAdd(counter, (unsigned int)kDynRows);
+        c0 = __shfl_sync(0xffffffffu, c0, 0);
+        r = c0;
+        rend = r + kDynRows < rows ? r + kDynRows : rows;
+        if (r >= rows) break;
+      }
+    } else if (r >= rows) {
+      break;
+    }
+    const int64_t rr = r;
+    r += DYN ? 1 : nw;
+    if (row_mask && !row_mask[rr]) continue;  // frozen row (warp-uniform)
+    const int64_t s = ptr[rr], e = ptr[rr + 1];
     VT acc = V16<T>::zero();
     for (int64_t base = s; base < e; base += 32 * CH) {
       int ci[CH];
@@ -373,14 +394,14 @@ spmm_kernel(int64_t rows, const int64_t* __restrict__ ptr, const int32_t* __rest
 #pragma unroll
     for (int o = LPN; o < 32; o <<= 1) V16<T>::add(acc, V16<T>::shfl_xor(acc, o));
     if (slot == 0) {
-      const T sc = scale[r];
-      T* op = out + r * B + sub * VW;
+      const T sc = scale[rr];
+      T* op = out + rr * B + sub * VW;
       const T* a = reinterpret_cast<const T*>(&acc);
       VT o;
       T* ov = reinterpret_cast<T*>(&o);
       if (SHIFT) {
-        const T d = dshift[r];
-        const T* yp = y + r * B + sub * VW;
+        const T d = dshift[rr];
+        const T* yp = y + rr * B + sub * VW;
 #pragma unroll
         for (int q = 0; q < VW; ++q) ov[q] = sc * a[q] - d * yp[q];
       } else {
@@ -531,7 +552,68 @@ extern "C" int sg_spectral_prepare(int64_t n, int64_t m, const int64_t* indptr, 
   return SG_OK;
 }
 
+template <int B, int VAR>
+int launch_spmm_dyn_v(int64_t rows, const int64_t* ptr, const int32_t* idx, const float* val, const float* in,
+                      float* out, const float* scale, const float* dshift, const float* y, cudaStream_t s,
+                      const unsigned char* mk, unsigned int* counter) {
+  auto run = [&](auto kern) -> int {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, 0) != cudaSuccess || per_sm < 1)
+      per_sm = 1;
+    const int64_t need = (rows + kDynRows * 8 - 1) / (kDynRows * 8);  // blocks that can get a chunk
+    int64_t grid = (int64_t)per_sm * sm_count();
+    if (grid > need) grid = need;
+    if (grid < 1) grid = 1;
+    if (cudaMemsetAsync(counter, 0, sizeof(unsigned int), s) != cudaSuccess) return SG_ERR_CUDA;
+    kern<<<(unsigned)grid, 256, 0, s>>>(rows, ptr, idx, val, in, out, scale, dshift, y, mk, counter);
+    return cudaGetLastError() == cudaSuccess ? SG_OK : SG_ERR_CUDA;
+  };
+  if (val) {
+    if (dshift) return run(spmm_kernel<float, B, true, true, VAR, true>);
+    return run(spmm_kernel<float, B, true, false, VAR, true>);
+  }
+  if (dshift) return run(spmm_kernel<float, B, false, true, VAR, true>);
+  return run(spmm_kernel<float, B, false, false, VAR, true>);
+}
+
+template <int B>
+int launch_spmm_dyn_b(int variant, int64_t rows, const int64_t* ptr, const int32_t* idx, const float* val,
+                      const float* in, float* out, const float* scale, const float* dshift, const float* y,
+                      cudaStream_t s, const unsigned char* mk, unsigned int* counter) {
+  switch (variant) {
+    case 0: return launch_spmm_dyn_v<B, 0>(rows, ptr, idx, val, in, out, scale, dshift, y, s, mk, counter);
+    case 1: return launch_spmm_dyn_v<B, 1>(rows, ptr, idx, val, in, out, scale, dshift, y, s, mk, counter);
+    case 2: return launch_spmm_dyn_v<B, 2>(rows, ptr, idx, val, in, out, scale, dshift, y, s, mk, counter);
+    case 3: return launch_spmm_dyn_v<B, 3>(rows, ptr, idx, val, in, out, scale, dshift, y, s, mk, counter);
+    case 4: return launch_spmm_dyn_v<B, 4>(rows, ptr, idx, val, in, out, scale, dshift, y, s, mk, counter);
+    case 5: return launch_spmm_dyn_v<B, 5>(rows, ptr, idx, val, in, out, scale, dshift, y, s, mk, counter);
+    case 6: return launch_spmm_dyn_v<B, 6>(rows, ptr, idx, val, in, out, scale, dshift, y, s, mk, counter);
+    case 7: return launch_spmm_dyn_v<B, 7>(rows, ptr, idx, val, in, out, scale, dshift, y, s, mk, counter);
+    default: return SG_ERR_ARG;
+  }
+}
+
 extern "C" int sg_spmm_variants(void) { return kSpmmVariants; }
+
+extern "C" int sg_spmm_dyn(int dtype, int block, int64_t rows, const int64_t* ptr, const int32_t* idx,
+                           const float* val, const void* in, void* out, const void* scale, const void* dshift,
+                           const void* y, int variant, const unsigned char* row_mask, unsigned int* counter,
+                           void* stream) {
+  if (rows < 0 || rows >= (int64_t(1) << 31) || !scale || (dshift && !y) || !counter || variant < 0 ||
+      variant >= kSpmmVariants || dtype != 0)
+    return SG_ERR_ARG;
+  if (rows == 0) return SG_OK;
+  cudaStream_t s = as_stream(stream);
+  const float *fi = (const float*)in, *fs = (const float*)scale, *fd = (const float*)dshift, *fy = (const float*)y;
+  float* fo = (float*)out;
+  switch (block) {
+    case 4: return launch_spmm_dyn_b<4>(variant, rows, ptr, idx, val, fi, fo, fs, fd, fy, s, row_mask, counter);
+    case 8: return launch_spmm_dyn_b<8>(variant, rows, ptr, idx, val, fi, fo, fs, fd, fy, s, row_mask, counter);
+    case 16: return launch_spmm_dyn_b<16>(variant, rows, ptr, idx, val, fi, fo, fs, fd, fy, s, row_mask, counter);
+    case 32: return launch_spmm_dyn_b<32>(variant, rows, ptr, idx, val, fi, fo, fs, fd, fy, s, row_mask, counter);
+    default: return SG_ERR_ARG;
+  }
+}
 
 extern "C" int sg_spmm_masked(int dtype, int block, int64_t rows, const int64_t* ptr, const int32_t* idx,
                               const float* val, const void* in, void* out, const void* scale, const void* dshift,

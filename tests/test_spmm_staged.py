@@ -136,3 +136,43 @@ def test_gather_ceiling_diagnostic_runs_without_output():
             assert float(sink.item()) == 0.0
     assert L.sg_gather_ceiling(0, 12, idx.size, d_idx.data_ptr(), table.data_ptr(), sink.data_ptr(), sh) == \
         _lib.SG_ERR_ARG
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("block,valued,shift,masked,variant", [(8, False, True, False, 0), (8, True, False, True, 3),
+                                                               (32, False, True, False, 1), (4, True, True, True, 6)])
+def test_dynamic_schedule_equals_static(block, valued, shift, masked, variant):
+    """sg_spmm_dyn sums each row in the same order as sg_spmm_masked: the
+    outputs are bitwise equal, masked rows untouched, on a skewed matrix."""
+    import torch
+    L = _lib.lib()
+    dev = torch.device("cuda", 0)
+    rng = np.random.default_rng(block + variant)
+    rows, cols = 200_000, 40_000
+    lens = np.minimum(rng.zipf(1.6, rows), 3000)            # heavy tail of long rows
+    row_of = np.repeat(np.arange(rows, dtype=np.int64), lens)
+    keys = np.unique(row_of * cols + rng.integers(0, cols, row_of.size))
+    indptr = np.zeros(rows + 1, np.int64)
+    np.cumsum(np.bincount(keys // cols, minlength=rows), out=indptr[1:])
+    idx = (keys % cols).astype(np.int32)
+    t = lambda a, dt=torch.float32: torch.from_numpy(np.ascontiguousarray(a)).to(dev, dt)  # noqa: E731
+    ip, ix = torch.from_numpy(indptr).to(dev), torch.from_numpy(idx).to(dev)
+    val = t(rng.integers(1, 5, idx.size)) if valued else None
+    inp = t(rng.standard_normal((cols, block)))
+    sc = t(rng.uniform(0.5, 2.0, rows))
+    dsh = t(rng.uniform(0.1, 1.0, rows)) if shift else None
+    y = t(rng.standard_normal((rows, block))) if shift else None
+    mask = torch.from_numpy((rng.random(rows) < 0.7).astype(np.uint8)).to(dev) if masked else None
+    o1 = torch.full((rows, block), 7.0, dtype=torch.float32, device=dev)
+    o2 = o1.clone()
+    cnt = torch.zeros(1, dtype=torch.int32, device=dev)
+    sh = torch.cuda.current_stream().cuda_stream
+    p = lambda x: None if x is None else x.data_ptr()  # noqa: E731
+    _lib.check(L.sg_spmm_masked(0, block, rows, ip.data_ptr(), ix.data_ptr(), p(val), inp.data_ptr(), o1.data_ptr(),
+                                sc.data_ptr(), p(dsh), p(y), -1, variant, p(mask), sh), "static")
+    _lib.check(L.sg_spmm_dyn(0, block, rows, ip.data_ptr(), ix.data_ptr(), p(val), inp.data_ptr(), o2.data_ptr(),
+                             sc.data_ptr(), p(dsh), p(y), variant, p(mask), cnt.data_ptr(), sh), "dynamic")
+    torch.cuda.synchronize()
+    assert torch.equal(o1, o2)
+    assert L.sg_spmm_dyn(1, block, rows, ip.data_ptr(), ix.data_ptr(), None, inp.data_ptr(), o2.data_ptr(),
+                         sc.data_ptr(), None, None, 0, None, cnt.data_ptr(), sh) == _lib.SG_ERR_ARG
