@@ -101,6 +101,8 @@ class GramOperator:
             val = self.csr.data.data_ptr() if self.csr.data is not None else None
             scale, dsh, yp = a.data_ptr(), dinv.data_ptr(), y.data_ptr()
             mask = self.row_mask.data_ptr() if self.row_mask is not None else None
+        if variant >= DYN and dtype_code != 0:
+            variant -= DYN  # the dynamic schedule exists for FP32 only: same gathers, static schedule
         if variant >= DYN:
             if self.counter is None:
                 self.counter = torch.zeros(2, dtype=torch.int32, device=self.a.device)
