@@ -1,8 +1,9 @@
 // Stable LSD radix sort of 64-bit keys with optional 64-bit payloads.
 //
 // One pass per 8-bit digit, three launches per pass:
-//   radix_hist     per tile of kTile keys, the count of each digit value,
-//                  written digit-major (hist[1 + d * ntiles + tile]);
+//   radix_hist     per tile of kTile keys, the count of each digit value
+//                  (per-warp shared counters, then summed), written
+//                  digit-major (hist[1 + d * ntiles + tile]);
 //   scan           inclusive prefix sum of the histogram, so hist[d * ntiles
 //                  + tile] becomes the global output offset of the tile's
 //                  first key with digit d (digits in order, tiles in order:
@@ -30,25 +31,32 @@ __device__ __forceinline__ int digit_of(uint64_t k, int shift, uint32_t mask) {
   return (int)((k >> shift) & mask);
 }
 
+// Per-warp shared counters (plain shared atomics: a warp's lanes collide only
+// when their digits are equal), summed over the warps at the end.  The keys
+// of one thread are loaded together (kItems loads in flight).
 __global__ void __launch_bounds__(kThreads) radix_hist(int64_t n, const uint64_t* __restrict__ keys, int shift,
                                                        uint32_t mask, int64_t ntiles, int64_t* __restrict__ hist) {
-  __shared__ int cnt[256];
-  for (int i = threadIdx.x; i < 256; i += kThreads) cnt[i] = 0;
+  __shared__ int cnt[kWarps][256];
+  for (int i = threadIdx.x; i < kWarps * 256; i += kThreads) (&cnt[0][0])[i] = 0;
   __syncthreads();
   const int64_t t = blockIdx.x, base = t * kTile;
-  const int lane = threadIdx.x & 31;
-  for (int i = threadIdx.x; i < kTile; i += kThreads) {
-    const int64_t e = base + i;
-    const bool valid = e < n;
-    const unsigned act = __ballot_sync(0xffffffffu, valid);
-    if (valid) {
-      const int d = digit_of(__ldg(keys + e), shift, mask);
-      const unsigned peers = __match_any_sync(act, d);
-      if (lane == __ffs(peers) - 1) atomicAdd(&cnt[d], __popc(peers));
-    }
+  const int w = threadIdx.x >> 5;
+  uint64_t k[kItems];
+#pragma unroll
+  for (int j = 0; j < kItems; ++j) {
+    const int64_t e = base + j * kThreads + threadIdx.x;
+    k[j] = e < n ? __ldg(keys + e) : 0;
   }
+#pragma unroll
+  for (int j = 0; j < kItems; ++j)
+    if (base + j * kThreads + threadIdx.x < n) atomicAdd(&cnt[w][digit_of(k[j], shift, mask)], 1);
   __syncthreads();
-  for (int d = threadIdx.x; d < 256; d += kThreads) hist[1 + (int64_t)d * ntiles + t] = cnt[d];
+  for (int d = threadIdx.x; d < 256; d += kThreads) {
+    int s = 0;
+#pragma unroll
+    for (int i = 0; i < kWarps; ++i) s += cnt[i][d];
+    hist[1 + (int64_t)d * ntiles + t] = s;
+  }
   if (t == 0 && threadIdx.x == 0) hist[0] = 0;
 }
 
