@@ -59,8 +59,22 @@ class _UploadPool:
             if cur is None or cur.numel() < buf.numel():
                 self._free[key] = buf
 
+    def clear(self) -> None:
+        """Drop the pooled buffers (their memory returns to torch's allocator)."""
+        with self._lock:
+            self._free.clear()
+
+    def pooled_bytes(self) -> int:
+        with self._lock:
+            return sum(b.numel() * b.element_size() for b in self._free.values())
+
 
 _UPLOADS = _UploadPool()
+
+
+def clear_upload_pool() -> None:
+    """Release the device buffers kept for host-to-device uploads."""
+    _UPLOADS.clear()
 
 
 def csr_to_device(X, device, borrowed: list | None = None) -> DeviceCSR:
