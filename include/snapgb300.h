@@ -291,6 +291,18 @@ int sg_spmm_masked(int dtype, int block, int64_t rows, const int64_t* ptr, const
                    const void* in, void* out, const void* scale, const void* dshift, const void* y, int grid,
                    int variant, const unsigned char* row_mask, void* stream);
 
+/* IDF weights from per-column cell counts (FP64, e.g. sg_col_counts of the */
+/* index pattern) with the rules of idf (embedding.rs:269-286): all counts   */
+/* equal -> 1, count 0 -> 1, count n -> n - 1, w = ln(n / count).  mm: two   */
+/* uint64 of scratch.                                                       */
+int sg_idf_from_counts(int64_t n, int64_t m, const double* counts, double* w, unsigned long long* mm,
+                       void* stream);
+
+/* rinv[i] = 1 / ||x_i ⊙ w||_2 over the CSR rows (normalize, embedding.rs:  */
+/* 315-326); a row with no weight sets SG_ERR_NUMERIC with its index.        */
+int sg_csr_row_norms(int64_t n, const int64_t* indptr, const int32_t* indices, const float* values,
+                     const double* w, double* rinv, int* status, unsigned long long* bad, void* stream);
+
 /* sg_spmm_masked on a persistent grid whose warps take 4 rows at a time    */
 /* from *counter (device, zeroed by this call on `stream`): rows of very     */
 /* different lengths leave no tail.  Same per-row arithmetic and result.     */

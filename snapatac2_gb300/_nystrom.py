@@ -4,9 +4,11 @@ Follows ``spectral_embedding_nystrom`` (``snapatac2-python/src/embedding.rs:61-1
 and ``nystrom`` (``embedding.rs:193-267``), then ``orthogonalize``
 (``snapatac2-python/python/snapatac2/tools/_embedding.py:397-413``):
 
-1. IDF weights over all cells; landmarks drawn uniformly, or with
+1. IDF weights over all cells (column cell counts, no transpose of the
+   whole matrix) and row norms; landmarks drawn uniformly, or with
    probability proportional to 1 / (degree - 1) (``sample_method="degree"``,
-   ``compute_degrees`` / ``compute_probs``, ``embedding.rs:328-365``);
+   ``compute_degrees`` / ``compute_probs``, ``embedding.rs:328-365``: this
+   one needs the full operator set-up, transpose included);
 2. the landmark rows, normalised with the global weights, embedded by the
    same matrix-free eigensolver as the full path (``spectral_mf``);
 3. every cell extended out of sample with two FP64 SpMM launches
@@ -73,6 +75,45 @@ def orthogonalize(evals: np.ndarray, q: torch.Tensor):
     return evals_new, q @ M
 
 
+def weights_and_norms(csr: DeviceCSR, feature_weights=None):
+    """(w, rinv) of all cells without the full operator: IDF from the
+    columns' cell counts (``sg_col_counts`` of the index pattern, then
+    ``sg_idf_from_counts``) unless weights are given, and the row norms
+    (``sg_csr_row_norms``).  No transpose of the whole matrix is built."""
+    L = _lib.lib()
+    dev = csr.indptr.device
+    n, m = csr.shape
+    sh = torch.cuda.current_stream(dev).cuda_stream
+    f64 = dict(dtype=torch.float64, device=dev)
+    st = _lib.DeviceStatus(dev)
+    if feature_weights is None:
+        counts = torch.empty(m, **f64)
+        scratch = torch.empty(m, dtype=torch.int64, device=dev)
+        _lib.check(L.sg_col_counts(int(csr.nnz), m, csr.indices.data_ptr() if csr.nnz else None, None, None,
+                                   counts.data_ptr(), scratch.data_ptr(), st.status_ptr, st.bad_ptr, sh),
+                   "sg_col_counts")
+        st.raise_if_error("column counts (column index out of range)")
+        w = torch.empty(m, **f64)
+        mm = torch.empty(2, dtype=torch.int64, device=dev)
+        _lib.check(L.sg_idf_from_counts(n, m, counts.data_ptr(), w.data_ptr(), mm.data_ptr(), sh), "sg_idf")
+    else:
+        w = torch.as_tensor(np.asarray(feature_weights, dtype=np.float64)).to(dev)
+        if w.numel() != m:
+            raise ValueError(f"feature_weights has {w.numel()} entries, expected {m}")
+    rinv = torch.empty(n, **f64)
+    _lib.check(L.sg_csr_row_norms(n, csr.indptr.data_ptr(), csr.indices.data_ptr() if csr.nnz else None,
+                                  None if csr.data is None else csr.data.data_ptr(), w.data_ptr(), rinv.data_ptr(),
+                                  st.status_ptr, st.bad_ptr, sh), "sg_csr_row_norms")
+    try:
+        st.raise_if_error("row norms", "cell")
+    except _lib.SnapGB300Error as e:
+        if e.code == _lib.SG_ERR_NUMERIC:
+            raise ValueError(f"cell {e.bad_index} has no selected features; the cosine operator is undefined "
+                             "(the reference produces NaN)") from e
+        raise
+    return w, rinv
+
+
 def spectral_nystrom(X, features=None, n_comps: int = 30, sample_size: int = 1000, *,
                      weighted_by_degree: bool = False, chunk_size: int = 20000, feature_weights=None,
                      landmarks=None, seed: int = 2023, random_state: int = 0, precision: str = "auto",
@@ -86,17 +127,20 @@ def spectral_nystrom(X, features=None, n_comps: int = 30, sample_size: int = 100
         csr = csr_to_device(X, dev, borrowed)
         csr = _eigen.select_columns(csr, features)
         n, m = csr.shape
-        op = _eigen.build_operator(csr, feature_weights)     # global IDF weights, row norms, degrees
-        if landmarks is None:
-            rng = np.random.default_rng(seed)
-            if weighted_by_degree:
-                inv = op.dinv.cpu().numpy()                   # 1 / (degree - 1)
-                landmarks = rng.choice(n, sample_size, replace=False, p=inv / inv.sum())
-            else:
-                landmarks = rng.choice(n, sample_size, replace=False)
+        if weighted_by_degree and landmarks is None:
+            # degrees need the column sums of all normalised rows: the full set-up (with its transpose)
+            op = _eigen.build_operator(csr, feature_weights)
+            w, rinv = op.w, op.rinv
+            inv = op.dinv.cpu().numpy()                       # 1 / (degree - 1)
+            del op
+            landmarks = np.random.default_rng(seed).choice(n, sample_size, replace=False, p=inv / inv.sum())
+        else:
+            w, rinv = weights_and_norms(csr, feature_weights)
+            if landmarks is None:
+                landmarks = np.random.default_rng(seed).choice(n, sample_size, replace=False)
         lm = torch.as_tensor(np.asarray(landmarks, dtype=np.int64)).to(dev)
         seed_csr = select_rows(csr, lm)
-        op_s = _eigen.build_operator(seed_csr, op.w)          # landmarks with the global weights
+        op_s = _eigen.build_operator(seed_csr, w)             # landmarks with the global weights
         if precision == "auto":
             from .tools import AUTO_FP64_CELLS
             precision = "fp64" if op_s.n < AUTO_FP64_CELLS else "mixed"
@@ -114,10 +158,10 @@ def spectral_nystrom(X, features=None, n_comps: int = 30, sample_size: int = 100
             inp = torch.zeros(op_s.n, blk, **f64)
             inp[:, :kc] = ev[:, c0:c0 + kc] * op_s.rinv.unsqueeze(1)
             W = torch.empty(m, blk, **f64)
-            _spmm64(m, op_s.colptr, op_s.rowidx, op_s.cvalues, inp, W, op.w, blk, sh)
-            W *= op.w.unsqueeze(1)
+            _spmm64(m, op_s.colptr, op_s.rowidx, op_s.cvalues, inp, W, w, blk, sh)
+            W *= w.unsqueeze(1)
             Q = torch.empty(n, blk, **f64)
-            _spmm64(n, csr.indptr, csr.indices, csr.data, W, Q, op.rinv, blk, sh)
+            _spmm64(n, csr.indptr, csr.indices, csr.data, W, Q, rinv, blk, sh)
             q[:, c0:c0 + kc] = Q[:, :kc]
         vt = torch.from_numpy(v).to(dev)
         for r0 in range(0, n, chunk_size):
@@ -130,7 +174,7 @@ def spectral_nystrom(X, features=None, n_comps: int = 30, sample_size: int = 100
             qc /= d.sqrt().unsqueeze(1)
         evals, evecs = orthogonalize(v, q)
         info = {"landmarks": int(lm.numel()), "landmark_solve": res.info}
-        del op, op_s, csr, seed_csr
+        del op_s, csr, seed_csr
     finally:
         release_uploads(borrowed)
     if return_info:

@@ -593,6 +593,64 @@ int launch_spmm_dyn_b(int variant, int64_t rows, const int64_t* ptr, const int32
   }
 }
 
+__global__ void count_minmax(int64_t m, const double* __restrict__ cnt, unsigned long long* mm) {
+  unsigned long long lo = ~0ull, hi = 0;
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < m; j += (int64_t)gridDim.x * blockDim.x) {
+    const unsigned long long c = (unsigned long long)cnt[j];
+    lo = c < lo ? c : lo;
+    hi = c > hi ? c : hi;
+  }
+  for (int o = 16; o; o >>= 1) {
+    const unsigned long long a = __shfl_xor_sync(0xffffffffu, lo, o), b = __shfl_xor_sync(0xffffffffu, hi, o);
+    lo = a < lo ? a : lo;
+    hi = b > hi ? b : hi;
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicMin(mm, lo);
+    atomicMax(mm + 1, hi);
+  }
+}
+
+// idf_kernel's rules from per-column cell counts instead of CSC column pointers
+__global__ void idf_from_counts(int64_t n, int64_t m, const double* __restrict__ cnt,
+                                const unsigned long long* __restrict__ mm, double* __restrict__ w) {
+  const bool equal = mm[0] == mm[1];
+  const double dn = (double)n;
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < m; j += (int64_t)gridDim.x * blockDim.x) {
+    if (equal) { w[j] = 1.0; continue; }
+    double c = cnt[j];
+    if (c == 0.0) c = 1.0;
+    else if (c == dn) c = dn - 1.0;
+    w[j] = log(dn / c);
+  }
+}
+
+__global__ void init_mm(unsigned long long* mm) { mm[0] = ~0ull; mm[1] = 0; }
+
+extern "C" int sg_idf_from_counts(int64_t n, int64_t m, const double* counts, double* w, unsigned long long* mm,
+                                  void* stream) {
+  if (n < 1 || m < 0 || (m > 0 && (!counts || !w || !mm))) return SG_ERR_ARG;
+  if (m == 0) return SG_OK;
+  cudaStream_t s = as_stream(stream);
+  const int g = grid_for(m, 256, 4 * sm_count());
+  init_mm<<<1, 1, 0, s>>>(mm);
+  count_minmax<<<g, 256, 0, s>>>(m, counts, mm);
+  idf_from_counts<<<g, 256, 0, s>>>(n, m, counts, mm, w);
+  SG_CHECK_LAUNCH();
+  return SG_OK;
+}
+
+extern "C" int sg_csr_row_norms(int64_t n, const int64_t* indptr, const int32_t* indices, const float* values,
+                                const double* w, double* rinv, int* status, unsigned long long* bad, void* stream) {
+  if (n < 0 || (n > 0 && (!indptr || !w || !rinv || !status))) return SG_ERR_ARG;
+  if (n == 0) return SG_OK;
+  cudaStream_t s = as_stream(stream);
+  rownorm_kernel<<<grid_for(n * 32, 256, 8 * sm_count()), 256, 0, s>>>(n, indptr, indices, values, w, rinv, status,
+                                                                      bad);
+  SG_CHECK_LAUNCH();
+  return SG_OK;
+}
+
 extern "C" int sg_spmm_variants(void) { return kSpmmVariants; }
 
 extern "C" int sg_spmm_dyn(int dtype, int block, int64_t rows, const int64_t* ptr, const int32_t* idx,

@@ -60,3 +60,21 @@ def test_gpu_spectral_sample_size_api():
     assert ad.obsm["X_spectral"].shape[0] == X.shape[0]
     with pytest.raises(ValueError):
         snap.tl.spectral(ad, features=None, sample_size=1)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("valued", [False, True])
+def test_gpu_light_setup_equals_operator(valued):
+    """IDF from column counts and the row norms, without the transpose, give
+    the full operator set-up's weights and norms bit for bit."""
+    import torch
+    from snapatac2_gb300 import _eigen
+    from snapatac2_gb300._nystrom import weights_and_norms
+    from snapatac2_gb300.tools import csr_to_device
+    X = _data()
+    if valued:
+        X.data = np.random.default_rng(3).integers(1, 4, X.nnz).astype(np.float64)
+    csr = csr_to_device(X, torch.device("cuda"))
+    w, rinv = weights_and_norms(csr)
+    op = _eigen.build_operator(csr)
+    assert torch.equal(w, op.w) and torch.equal(rinv, op.rinv)
