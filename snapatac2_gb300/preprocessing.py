@@ -16,7 +16,7 @@ import scipy.sparse as sp
 import torch
 
 from . import _binning
-from ._anndata import AnnData, is_anndata
+from ._anndata import AnnData
 from .genome import ChromSizes, TileNames
 
 FRAGMENT_SINGLE = "fragment_single"   # snapatac2-core/src/feature_count/mod.rs:20
