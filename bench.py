@@ -954,7 +954,7 @@ def run_import(args):
         frs = S.make_fragments(args.import_cpu_cells, g, seed=1)
         txt = bytes(S.fragment_text(frs, g, order="position").numpy())
         t0 = time.perf_counter()
-        ref = ofr.import_fragments(txt, genome, **kw)
+        ref = ofr.import_fragments_c(txt, genome, **kw)
         cs = time.perf_counter() - t0
         nl = txt.count(b"\n")
         gpu_s = _import.import_text(txt, genome, **kw)
@@ -962,7 +962,7 @@ def run_import(args):
                 and np.array_equal(gpu_s.data, ref["data"]) and np.array_equal(gpu_s.frac_dup, ref["frac_dup"]))
         cpu = {"value": nl / cs, "unit": "fragments/s", "cores": 1, "kind": "port",
                "sample": f"{args.import_cpu_cells}-cell file of the same generator ({nl} lines), "
-                         "oracle restatement of the reference import in Python",
+                         "oracle restatement of the reference import in C (one thread, qsort)",
                "sample_identical_to_oracle": bool(same)}
     alg = nbytes + nnz * 12 + (K + 1) * 8 + K * 32
     peak, peak_kind = peaks()

@@ -223,3 +223,68 @@ def import_fragments(text: bytes, chrom_sizes: dict, *, min_num_fragments: int =
         frac_mito=np.array([q[2] for q in qc], dtype=np.float64),
     )
     return out
+
+
+# ---- the same import in C (oracle/fragments.c), for a CPU baseline of realistic speed ----
+
+def import_fragments_c(text: bytes, chrom_sizes: dict, *, min_num_fragments: int = 200,
+                       sorted_by_barcode: bool = True, whitelist=None, chrM=("chrM", "M"),
+                       shift_left: int = 0, shift_right: int = 0) -> dict:
+    """``import_fragments`` through oracle/fragments.c; same result dict."""
+    import ctypes
+    from ._build import load_lib
+
+    class Out(ctypes.Structure):
+        _fields_ = [("n_cells", ctypes.c_int64), ("nnz", ctypes.c_int64), ("paired", ctypes.c_int64),
+                    ("bad_line", ctypes.c_int64), ("error", ctypes.c_int64)] + \
+                   [(k, ctypes.c_void_p) for k in ("indptr", "indices", "data", "bc_off", "bc_len", "n_fragment",
+                                                     "frac_dup", "frac_mito")]
+
+    if len(chrom_sizes) == 0:
+        raise ValueError("chrom_size cannot be empty")
+    lib = load_lib("fragments")
+    f = lib.oracle_import
+    P, I64 = ctypes.c_void_p, ctypes.c_int64
+    f.restype = I64
+    f.argtypes = [ctypes.c_char_p, I64, ctypes.c_char_p, P, P, P, P, ctypes.c_int, ctypes.c_char_p, P, I64,
+                  ctypes.c_int, ctypes.c_uint64, ctypes.c_int, I64, I64, ctypes.POINTER(Out)]
+    lib.oracle_import_free.argtypes = [ctypes.POINTER(Out)]
+    names = sorted(chrom_sizes, key=lambda s: s.encode())
+    nb = [n.encode() for n in names]
+    coff = np.concatenate([[0], np.cumsum([len(b) for b in nb])]).astype(np.int64)
+    csize = np.array([int(chrom_sizes[n]) for n in names], dtype=np.uint64)
+    cbase = np.concatenate([[0], np.cumsum(csize)[:-1]]).astype(np.uint64)
+    mito = {c.encode() for c in chrM}
+    cmito = np.array([b in mito for b in nb], dtype=np.uint8)
+    wl = sorted({w.encode() if isinstance(w, str) else bytes(w) for w in whitelist}) if whitelist is not None else []
+    woff = np.concatenate([[0], np.cumsum([len(w) for w in wl])]).astype(np.int64)
+    o = Out()
+    err = f(text, len(text), b"".join(nb), coff.ctypes.data, csize.ctypes.data, cbase.ctypes.data, cmito.ctypes.data,
+            len(nb), b"".join(wl), woff.ctypes.data, len(wl), int(whitelist is not None),
+            int(max(min_num_fragments, 0)), int(bool(sorted_by_barcode)), int(shift_left), int(shift_right),
+            ctypes.byref(o))
+    if err:
+        raise ImportError_(f"line {o.bad_line}: import error {err}")
+    paired = bool(o.paired == 1)
+    out = {"key": None, "obs_names": [], "chrom_names": names, "chrom_sizes": [int(x) for x in csize],
+           "genome_size": int(csize.sum()), "paired": paired}
+    try:
+        K, nnz = int(o.n_cells), int(o.nnz)
+        if K == 0:
+            return out
+        arr = lambda ptr, n, dt: np.ctypeslib.as_array(ctypes.cast(ptr, ctypes.POINTER(dt)), shape=(n,)).copy()  # noqa: E731
+        offs = arr(o.bc_off, K, ctypes.c_int64)
+        lens = arr(o.bc_len, K, ctypes.c_int32)
+        data = arr(o.data, nnz, ctypes.c_int64) if nnz else np.zeros(0, np.int64)
+        out.update(
+            key="fragment_paired" if paired else "fragment_single",
+            obs_names=[text[a:a + b].decode() for a, b in zip(offs.tolist(), lens.tolist())],
+            indptr=arr(o.indptr, K + 1, ctypes.c_int64),
+            indices=arr(o.indices, nnz, ctypes.c_int64) if nnz else np.zeros(0, np.int64),
+            data=data.astype(np.uint32 if paired else np.int32),
+            n_fragment=arr(o.n_fragment, K, ctypes.c_uint64),
+            frac_dup=arr(o.frac_dup, K, ctypes.c_double),
+            frac_mito=arr(o.frac_mito, K, ctypes.c_double))
+        return out
+    finally:
+        lib.oracle_import_free(ctypes.byref(o))

@@ -268,3 +268,46 @@ def test_gpu_radix_sort_stable(n, bits):
     order = np.argsort(masked, kind="stable")
     np.testing.assert_array_equal(rv.cpu().numpy().view(np.uint64), order.astype(np.uint64))
     np.testing.assert_array_equal(rk.cpu().numpy().view(np.uint64), keys[order])
+
+
+# ---- the two oracle restatements (Python, C) agree (CPU) ---------------------------
+
+def _same_oracle(a, b):
+    assert a["key"] == b["key"] and a["obs_names"] == b["obs_names"] and a["paired"] == b["paired"]
+    if a["key"] is None:
+        return
+    for k in ("indptr", "indices", "data", "n_fragment", "frac_dup", "frac_mito"):
+        assert a[k].dtype == b[k].dtype, k
+        np.testing.assert_array_equal(a[k], b[k], err_msg=k)
+
+
+@pytest.mark.parametrize("case", range(len(CASES)))
+def test_c_oracle_matches_python_oracle(case):
+    c = CASES[case]
+    text, genome = _synthetic(n_cells=25, order=c["order"], single_end=c.get("single_end", False), seed=case + 40)
+    try:
+        ref = ofr.import_fragments(text, genome, **c["kw"])
+    except ValueError:  # the data make the reference panic (e.g. a shift past a chromosome end): so must C
+        with pytest.raises(ValueError):
+            ofr.import_fragments_c(text, genome, **c["kw"])
+        return
+    _same_oracle(ref, ofr.import_fragments_c(text, genome, **c["kw"]))
+
+
+def test_c_oracle_edge_files_and_errors():
+    small = [
+        _text(["chr1\t1\t5\tA\t1", "chr1\t2\t6\tA\t1"], nl="\r\n", trailing=False),
+        _text(["# only a comment"]), b"",
+        _text(["chr1\t1\t5\tA\t1", "chr1\t4\t4\tB\t1", "chrUn\t1\t5\tC\t1"]),
+        _text(["chr1\t1\t5\tA\t1\t.\textra\tfields", "chr2\t1\t2\tA"]),
+        _text(["chr1\t1\t5\tB\t0", "chrM\t1\t2\tA\t0"]),
+        _text(["chr1\t9\t5\tA\t1\t-", "chr2\t0\t7\tA\t1\t+"]),
+    ]
+    for t in small:
+        for kw in (dict(min_num_fragments=0), dict(min_num_fragments=1, sorted_by_barcode=False),
+                   dict(min_num_fragments=0, whitelist=["A"])):
+            _same_oracle(ofr.import_fragments(t, GENOME, **kw), ofr.import_fragments_c(t, GENOME, **kw))
+    for lines in (["chr1\t1\t5\tB\t1", "chr1\t1\t5\tA\t1", "chr1\t2\t5\tB\t1"], ["chr1\tx\t5\tA"],
+                  ["chr1\t1\t5\t.\t1"], ["chr10\t3000\t3005\tA\t1"], ["chr1\t9\t5\tA\t1"]):
+        with pytest.raises(ValueError):
+            ofr.import_fragments_c(_text(lines), GENOME, min_num_fragments=0)
