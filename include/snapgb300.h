@@ -210,6 +210,43 @@ int sg_radix_sort_u64(int64_t n, uint64_t* keys, uint64_t* vals, uint64_t* keys_
                       int begin_bit, int end_bit, void* scratch, int* result_in_alt, void* stream);
 
 /* ------------------------------------------------------------------------ */
+/* Row and segment steps around the main kernels                            */
+/* ------------------------------------------------------------------------ */
+
+/* Rows `rows[k]` of a CSR, in that order (the Nyström landmark matrix,     */
+/* `slice(&[selected_samples, ...])`, snapatac2-python/src/embedding.rs:95-99). */
+/* sg_csr_row_ptr writes out_ptr[k + 1] (scan_scratch: sg_scan_scratch_bytes(k)); */
+/* sg_csr_copy_rows then copies indices (and values when not NULL).        */
+int sg_csr_row_ptr(int64_t k, const int64_t* rows, const int64_t* indptr, int64_t* out_ptr, void* scan_scratch,
+                   void* stream);
+int sg_csr_copy_rows(int64_t k, const int64_t* rows, const int64_t* indptr, const int32_t* indices,
+                     const float* values, const int64_t* out_ptr, int32_t* out_idx, float* out_val, void* stream);
+
+/* dst[dst_off[i] ..] = src[off[i] .. off[i] + len[i]) for i < k: the cell  */
+/* barcodes of an import gathered out of the fragment text.                 */
+int sg_gather_bytes(int64_t k, const int64_t* off, const int32_t* len, const int64_t* dst_off, const uint8_t* src,
+                    uint8_t* dst, void* stream);
+
+/* Gene-level counts: per row, the maximum count over the regions mapped to */
+/* each gene (GeneCount::get_values, snapatac2-core/src/feature_count/      */
+/* counter.rs:270-283).  Input: a region-count CSR (n rows, nnz entries,    */
+/* region indices, uint32 counts) and region_gene[region].  Output: out_ptr */
+/* [n + 1], out_idx / out_val (room for nnz entries; genes ascending within */
+/* a row), *n_out (host) = entries written.  Synchronises the stream.       */
+int64_t sg_gene_max_scratch_bytes(int64_t nnz);
+int sg_gene_max(int64_t n, const int64_t* indptr, const int32_t* region, const uint32_t* counts,
+                const int32_t* region_gene, int64_t nnz, void* scratch, int64_t scratch_bytes, int64_t* out_ptr,
+                int32_t* out_idx, int32_t* out_val, int64_t* n_out, void* stream);
+
+/* Nyström's per-chunk rescaling (the embedded Python of `nystrom`,         */
+/* snapatac2-python/src/embedding.rs:222-229) of q[n][k] (FP64, k <= 256) in */
+/* place, chunks of `chunk` rows: t = λ ⊙ Σ_chunk q, d = q t, d <= 0 -> the  */
+/* chunk's smallest positive d, q /= sqrt(d).  A chunk with no positive d   */
+/* where one is needed sets status SG_ERR_NUMERIC, bad = its first row.     */
+int sg_nystrom_rescale(int64_t n, int k, double* q, const double* evals, int64_t chunk, int* status,
+                       unsigned long long* bad, void* stream);
+
+/* ------------------------------------------------------------------------ */
 /* Feature selection -- the `count` vector of select_features              */
 /*   (snapatac2-python/python/snapatac2/preprocessing/_basic.py:1053-1056:   */
 /*   FP64 column sums of X).  The ranking itself (_basic.py:952-967, NumPy  */

@@ -19,7 +19,7 @@ Restates ``snap.pp.make_gene_matrix`` over fragments:
   ``RegionCounter`` (oracle ``regions.region_counts``); "transcript" columns
   are region indices under the transcript ids, "gene" columns take, per
   gene name, the maximum over the regions whose index, read as a transcript
-  index, names that gene (``GeneCount::get_values``, counter.rs:262-276),
+  index, names that gene (``GeneCount::get_values``, counter.rs:270-283),
   genes numbered by first appearance.
 """
 from __future__ import annotations

@@ -37,13 +37,20 @@ def nystrom(X: sp.csr_matrix, landmarks, n_comps: int = 30, chunk_size: int = 20
     outs = []
     for r0 in range(0, X.shape[0], chunk_size):
         sample = osp.normalize(sp.csr_matrix(X[r0:r0 + chunk_size]), w)
-        q = sample @ (seed.T @ evecs)
-        t = q.sum(axis=0) * v
-        dd = q @ t.reshape((-1, 1))
-        dd[dd <= 0] = np.min(dd[dd > 0])
-        np.divide(q, np.sqrt(dd), out=q)
-        outs.append(q)
+        outs.append(rescale_chunk(sample @ (seed.T @ evecs), v))
     return v, np.vstack(outs)
+
+
+def rescale_chunk(q, v):
+    """One chunk of the embedded Python of ``nystrom`` (embedding.rs:224-228):
+    d = q (Σ q ⊙ λ), d <= 0 -> min positive d (raises when there is none),
+    q / sqrt(d).  Returns a new array."""
+    q = np.array(q, dtype=np.float64)
+    t = q.sum(axis=0) * v
+    dd = q @ t.reshape((-1, 1))
+    dd[dd <= 0] = np.min(dd[dd > 0])
+    np.divide(q, np.sqrt(dd), out=q)
+    return q
 
 
 def orthogonalize(evals, evecs):

@@ -8,11 +8,12 @@ The annotation is read on the host (GTF / GFF3 "transcript" records,
 (``Promoters::new``, ``genome.rs:198-232``) are counted by the GPU region
 counter (``sg_region_plan`` / ``sg_region_run``), and the gene level keeps,
 per gene, the maximum over its regions (``GeneCount::get_values``,
-``snapatac2-core/src/feature_count/counter.rs:262-276``) with a device-side
-sort and segment maximum.
+``snapatac2-core/src/feature_count/counter.rs:270-283``) on the device
+(``sg_gene_max``: radix sort of (cell, gene) keys, segment maximum).
 """
 from __future__ import annotations
 
+import ctypes
 import gzip
 from urllib.parse import unquote
 
@@ -95,26 +96,31 @@ def promoter_regions(transcripts, upstream: int, downstream: int, include_gene_b
     return regs
 
 
-def gene_max(indptr: torch.Tensor, indices: torch.Tensor, data: torch.Tensor, region_gene: torch.Tensor,
-             n_genes: int):
-    """Per row, the maximum count over the regions of each gene: columns
-    mapped to genes, (row, gene) keys sorted, segment maximum."""
+def gene_max(indptr: torch.Tensor, indices: torch.Tensor, data: torch.Tensor, region_gene: torch.Tensor):
+    """Per row, the maximum count over the regions of each gene
+    (``sg_gene_max``: (row, gene) keys radix-sorted with their counts, runs
+    reduced by maximum).  Returns (indptr int64, gene int32, count int32)."""
+    from . import _lib
+    L = _lib.lib()
     dev = indptr.device
     n = indptr.numel() - 1
-    if indices.numel() == 0:
-        return torch.zeros(n + 1, dtype=torch.int64, device=dev), indices.to(torch.int64), data
-    row = torch.repeat_interleave(torch.arange(n, device=dev), indptr[1:] - indptr[:-1])
-    gene = region_gene[indices.long()]
-    key = row * n_genes + gene
-    key, order = torch.sort(key)
-    val = data.long()[order]
-    uk, inv = torch.unique_consecutive(key, return_inverse=True)
-    mx = torch.zeros(uk.numel(), dtype=torch.int64, device=dev).scatter_reduce(0, inv, val, "amax",
-                                                                                 include_self=False)
-    urow = uk // n_genes
-    ptr = torch.zeros(n + 1, dtype=torch.int64, device=dev)
-    ptr[1:] = torch.cumsum(torch.bincount(urow, minlength=n), 0)
-    return ptr, uk % n_genes, mx.to(torch.int32)
+    nnz = int(indices.numel())
+    sh = torch.cuda.current_stream(dev).cuda_stream
+    nbytes = int(L.sg_gene_max_scratch_bytes(nnz))
+    scratch = torch.empty(max(nbytes, 16), dtype=torch.uint8, device=dev)
+    out_ptr = torch.empty(n + 1, dtype=torch.int64, device=dev)
+    out_idx = torch.empty(max(nnz, 1), dtype=torch.int32, device=dev)
+    out_val = torch.empty(max(nnz, 1), dtype=torch.int32, device=dev)
+    n_out = ctypes.c_int64(0)
+    idx, val, rg = indices.contiguous(), data.contiguous(), region_gene.contiguous()
+    if idx.dtype != torch.int32 or val.element_size() != 4 or rg.dtype != torch.int32:
+        raise ValueError("gene_max: int32 region indices and region_gene, 32-bit counts expected")
+    _lib.check(L.sg_gene_max(n, indptr.data_ptr(), idx.data_ptr() if nnz else None,
+                             val.data_ptr() if nnz else None, rg.data_ptr() if rg.numel() else None, nnz,
+                             scratch.data_ptr(), nbytes, out_ptr.data_ptr(), out_idx.data_ptr(), out_val.data_ptr(),
+                             ctypes.byref(n_out), sh), "sg_gene_max")
+    u = int(n_out.value)
+    return out_ptr, out_idx[:u], out_val[:u]
 
 
 def make_gene_matrix(adata, gene_anno, *, inplace: bool = False, file=None, backend="hdf5", chunk_size: int = 500,
@@ -164,8 +170,8 @@ def make_gene_matrix(adata, gene_anno, *, inplace: bool = False, file=None, back
         names = list(gidx)
         # region k is read as transcript k (the reference's indexing; regions repeat-free)
         region_gene = torch.tensor([gidx[transcripts[k]["gene_name"]] for k in range(len(rs.names))],
-                                   dtype=torch.int64, device=dev)
-        ip, ix, dv = gene_max(res.indptr, res.indices, res.data, region_gene, max(len(names), 1))
+                                   dtype=torch.int32, device=dev)
+        ip, ix, dv = gene_max(res.indptr, res.indices, res.data, region_gene)
         var = None
     X = sp.csr_matrix((dv.cpu().numpy().view(np.uint32), ix.cpu().numpy(), ip.cpu().numpy()),
                       shape=(res.shape[0], len(names)))

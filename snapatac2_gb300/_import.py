@@ -246,17 +246,22 @@ def import_text(text: bytes | np.ndarray | torch.Tensor, chrom_sizes, *, min_num
 
 
 def _gather_barcodes(d_text: torch.Tensor, offs: np.ndarray, lens: np.ndarray) -> bytes:
-    """The kept cells' barcode bytes, concatenated, read from the device."""
+    """The kept cells' barcode bytes, concatenated, read from the device
+    (``sg_gather_bytes`` into one buffer, one copy back)."""
     if offs.size == 0:
         return b""
+    L = _lib.lib()
     dev = d_text.device
-    starts = torch.from_numpy(offs).to(dev)
-    ln = torch.from_numpy(lens).to(dev)
+    dst = np.zeros(offs.size, dtype=np.int64)
+    np.cumsum(lens[:-1], out=dst[1:])
     total = int(lens.sum())
-    seg = torch.repeat_interleave(torch.arange(offs.size, device=dev), ln)
-    first = torch.cumsum(ln, 0) - ln
-    idx = starts[seg] + (torch.arange(total, device=dev) - first[seg])
-    return d_text[idx].cpu().numpy().tobytes()
+    meta = torch.from_numpy(np.concatenate([offs.astype(np.int64), dst])).to(dev)
+    ln = torch.from_numpy(lens.astype(np.int32)).to(dev)
+    out = torch.empty(max(total, 1), dtype=torch.uint8, device=dev)
+    sh = torch.cuda.current_stream(dev).cuda_stream
+    _lib.check(L.sg_gather_bytes(offs.size, meta.data_ptr(), ln.data_ptr(), meta.data_ptr() + 8 * offs.size,
+                                 d_text.data_ptr(), out.data_ptr(), sh), "sg_gather_bytes")
+    return out[:total].cpu().numpy().tobytes()
 
 
 def to_anndata(res: ImportResult, adata=None):

@@ -57,6 +57,12 @@ SIGNATURES: dict[str, tuple] = {
     "sg_frag_import": (_I32, [_P, _I64, _P, _I64, _P, _P, _P, _P, _P, _I32, ctypes.c_uint64, _P, _P, _I64, _I32,
                               ctypes.c_uint64, _I32, _I64, _I64, ctypes.c_uint64, _P, _I64, _P, _P]),
     "sg_frag_emit": (_I32, [_P, _I64, _I64, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
+    "sg_csr_row_ptr": (_I32, [_I64, _P, _P, _P, _P, _P]),
+    "sg_csr_copy_rows": (_I32, [_I64, _P, _P, _P, _P, _P, _P, _P, _P]),
+    "sg_gather_bytes": (_I32, [_I64, _P, _P, _P, _P, _P, _P]),
+    "sg_gene_max_scratch_bytes": (_I64, [_I64]),
+    "sg_gene_max": (_I32, [_I64, _P, _P, _P, _P, _I64, _P, _I64, _P, _P, _P, _P, _P]),
+    "sg_nystrom_rescale": (_I32, [_I64, _I32, _P, _P, _I64, _P, _P, _P]),
     "sg_radix_scratch_bytes": (_I64, [_I64]),
     "sg_radix_sort_u64": (_I32, [_I64, _P, _P, _P, _P, _I32, _I32, _P, _P, _P]),
     "sg_csr_select_cols": (_I32, [_I64, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
@@ -116,6 +122,7 @@ KERNELS_PER_CALL = {
     "sg_adjoint_stage1": 1, "sg_adjoint_stage2": 1, "sg_adjoint_stage3": 1, "sg_adjoint_final": 1,
     "sg_square_values": 1,
     "sg_frag_count_lines": 4, "sg_frag_index_lines": 1, "sg_region_plan": 4, "sg_region_run": 5,
+    "sg_csr_row_ptr": 4, "sg_csr_copy_rows": 1, "sg_gather_bytes": 1, "sg_nystrom_rescale": 1,
 }
 
 _lock = threading.Lock()

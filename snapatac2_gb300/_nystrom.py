@@ -35,17 +35,46 @@ from ._binning import DeviceCSR
 
 
 def select_rows(csr: DeviceCSR, rows: torch.Tensor) -> DeviceCSR:
-    """The CSR rows ``rows`` (in that order), on the device."""
-    ip = csr.indptr
-    lens = (ip[1:] - ip[:-1])[rows]
-    ptr = torch.zeros(rows.numel() + 1, dtype=torch.int64, device=ip.device)
-    ptr[1:] = torch.cumsum(lens, 0)
-    total = int(ptr[-1].item())
-    src0 = torch.repeat_interleave(ip[:-1][rows], lens)
-    off = torch.arange(total, device=ip.device) - torch.repeat_interleave(ptr[:-1], lens)
-    pos = src0 + off
-    data = None if csr.data is None else csr.data[pos]
-    return DeviceCSR(ptr, csr.indices[pos].contiguous(), data, (int(rows.numel()), csr.shape[1]))
+    """The CSR rows ``rows`` (int64, in that order), on the device
+    (``sg_csr_row_ptr`` then ``sg_csr_copy_rows``)."""
+    L = _lib.lib()
+    dev = csr.indptr.device
+    k = int(rows.numel())
+    sh = torch.cuda.current_stream(dev).cuda_stream
+    if rows.dtype != torch.int64:
+        raise ValueError("row indices must be int64")
+    if csr.data is not None and csr.data.element_size() != 4:
+        raise ValueError("select_rows: 32-bit values expected")
+    ptr = torch.empty(k + 1, dtype=torch.int64, device=dev)
+    scan = torch.empty(max(int(L.sg_scan_scratch_bytes(k)), 16), dtype=torch.uint8, device=dev)
+    _lib.check(L.sg_csr_row_ptr(k, rows.data_ptr() if k else None, csr.indptr.data_ptr(), ptr.data_ptr(),
+                                scan.data_ptr(), sh), "sg_csr_row_ptr")
+    total = int(ptr[k].item())
+    idx = torch.empty(max(total, 1), dtype=torch.int32, device=dev)
+    val = None if csr.data is None else torch.empty(max(total, 1), dtype=csr.data.dtype, device=dev)
+    _lib.check(L.sg_csr_copy_rows(k, rows.data_ptr() if k else None, csr.indptr.data_ptr(),
+                                  csr.indices.data_ptr() if csr.nnz else idx.data_ptr(),
+                                  None if val is None else csr.data.data_ptr(), ptr.data_ptr(), idx.data_ptr(),
+                                  None if val is None else val.data_ptr(), sh), "sg_csr_copy_rows")
+    return DeviceCSR(ptr, idx[:total], None if val is None else val[:total], (k, csr.shape[1]))
+
+
+def rescale_chunks(q: torch.Tensor, evals: torch.Tensor, chunk_size: int) -> None:
+    """Nyström's per-chunk rescaling of q (n x k, FP64) in place
+    (``sg_nystrom_rescale``; the embedded Python of ``embedding.rs:222-229``)."""
+    L = _lib.lib()
+    n, k = q.shape
+    st = _lib.DeviceStatus(q.device)
+    _lib.check(L.sg_nystrom_rescale(n, k, q.data_ptr(), evals.data_ptr(), int(chunk_size), st.status_ptr,
+                                    st.bad_ptr, torch.cuda.current_stream(q.device).cuda_stream),
+               "sg_nystrom_rescale")
+    try:
+        st.raise_if_error("nystrom rescale", "row")
+    except _lib.SnapGB300Error as e:
+        if e.code == _lib.SG_ERR_NUMERIC:
+            raise ValueError(f"the chunk starting at cell {e.bad_index} has no positive degree estimate "
+                             "(the reference raises in np.min)") from e
+        raise
 
 
 def _spmm64(rows, ptr, idx, val, inp, out, scale, block, stream):
@@ -138,7 +167,10 @@ def spectral_nystrom(X, features=None, n_comps: int = 30, sample_size: int = 100
             w, rinv = weights_and_norms(csr, feature_weights)
             if landmarks is None:
                 landmarks = np.random.default_rng(seed).choice(n, sample_size, replace=False)
-        lm = torch.as_tensor(np.asarray(landmarks, dtype=np.int64)).to(dev)
+        lm_h = np.asarray(landmarks, dtype=np.int64).ravel()
+        if lm_h.size == 0 or lm_h.min() < 0 or lm_h.max() >= n:
+            raise ValueError(f"landmarks must be non-empty row indices in [0, {n})")
+        lm = torch.from_numpy(lm_h).to(dev)
         seed_csr = select_rows(csr, lm)
         op_s = _eigen.build_operator(seed_csr, w)             # landmarks with the global weights
         if precision == "auto":
@@ -163,15 +195,7 @@ def spectral_nystrom(X, features=None, n_comps: int = 30, sample_size: int = 100
             Q = torch.empty(n, blk, **f64)
             _spmm64(n, csr.indptr, csr.indices, csr.data, W, Q, rinv, blk, sh)
             q[:, c0:c0 + kc] = Q[:, :kc]
-        vt = torch.from_numpy(v).to(dev)
-        for r0 in range(0, n, chunk_size):
-            qc = q[r0:r0 + chunk_size]
-            t = qc.sum(0) * vt
-            d = qc @ t
-            pos = d > 0
-            if bool((~pos).any()):
-                d = torch.where(pos, d, d[pos].min())
-            qc /= d.sqrt().unsqueeze(1)
+        rescale_chunks(q, torch.from_numpy(v).to(dev), chunk_size)
         evals, evecs = orthogonalize(v, q)
         info = {"landmarks": int(lm.numel()), "landmark_solve": res.info}
         del op_s, csr, seed_csr
