@@ -162,6 +162,18 @@ def peaks():
 
 
 # --------------------------------------------------------------------------
+def host_threads() -> dict:
+    """The host's core count and the BLAS pools' thread counts (ARPACK's
+    dense steps run in BLAS), recorded beside every CPU baseline."""
+    blas = None
+    try:
+        from threadpoolctl import threadpool_info
+        blas = sorted({int(p.get("num_threads", 0)) for p in threadpool_info() if p.get("user_api") == "blas"})
+    except Exception:  # noqa: BLE001 - threadpoolctl is optional on the GPU host
+        pass
+    return {"host_cores": os.cpu_count(), "blas_threads": blas}
+
+
 def cpu_reference_sample(n_cells: int, args, seed: int):
     """The reference's arithmetic (oracle restatement, SciPy ARPACK) on a
     sample of the same generator; returns (seconds, n_cells)."""
@@ -194,7 +206,8 @@ def run_reference(args):
                                f"spectral n_comps={args.ncomps}", "sample_cells": args.cpu_sample_cells},
         "cpu_baseline": {"value": value, "unit": "cells/s", "cores": 1, "kind": "port",
                          "sample": f"{args.cpu_sample_cells}-cell sample of the same generator per step; "
-                                   "SciPy ARPACK eigsh with single-threaded sparse matvec, as the reference"},
+                                   "SciPy ARPACK eigsh with single-threaded sparse matvec, as the reference",
+                         **host_threads()},
         "e2e": {"value": value, "unit": "cells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -530,7 +543,8 @@ def run_gpu(args):
         dt, ns = cpu_reference_sample(args.cpu_sample_cells, args, seed=100)
         cpu = {"value": ns / dt, "unit": "cells/s", "cores": 1, "kind": "port",
                "sample": f"{ns} cells of the same generator ({args.features} features, ~{int(args.nnz)} nnz/cell): "
-                         "IDF/normalise/degree + SciPy ARPACK eigsh (single-threaded sparse matvec, as the reference)"}
+                         "IDF/normalise/degree + SciPy ARPACK eigsh (single-threaded sparse matvec, as the reference)",
+               **host_threads()}
     info = infos[-1]
     line = {
         "metric": METRIC, "value": value, "unit": "cells/s", "n_gpus": world, "steps": args.steps,
