@@ -244,10 +244,23 @@ def spmm_bytes(op: "GramOperator", dtype_code: int, block: int) -> tuple[int, in
     return t_pass, x_pass
 
 
+def check_column_indices(csr: DeviceCSR) -> None:
+    """Raise ValueError unless every column index lies in [0, m): kernels
+    that look a column up in a per-column table (the column map of the
+    selection, the weights of the row norms) read it unchecked.  SciPy's CSR
+    constructor does not check index bounds by default."""
+    if csr.nnz == 0:
+        return
+    lo, hi = int(csr.indices.min()), int(csr.indices.max())
+    if lo < 0 or hi >= csr.shape[1]:
+        raise ValueError(f"X must be CSR with column indices in [0, {csr.shape[1]}); found {lo}..{hi}")
+
+
 def select_columns(csr: DeviceCSR, features: np.ndarray | None) -> DeviceCSR:
     """X[:, features] on the GPU (embedding.rs:36-41)."""
     if features is None:
         return csr
+    check_column_indices(csr)
     L = _lib.lib()
     dev = csr.indptr.device
     n, mfull = csr.shape

@@ -126,6 +126,7 @@ def weights_and_norms(csr: DeviceCSR, feature_weights=None):
         mm = torch.empty(2, dtype=torch.int64, device=dev)
         _lib.check(L.sg_idf_from_counts(n, m, counts.data_ptr(), w.data_ptr(), mm.data_ptr(), sh), "sg_idf")
     else:
+        _eigen.check_column_indices(csr)       # no column count pass to check them
         w = torch.as_tensor(np.asarray(feature_weights, dtype=np.float64)).to(dev)
         if w.numel() != m:
             raise ValueError(f"feature_weights has {w.numel()} entries, expected {m}")

@@ -1,7 +1,7 @@
 """Host-side logic of the gene / peak matrices and the import (CPU): the
 product's annotation reader and promoter regions against the oracle's, region
-strings, the per-chromosome region index handed to the region counter, and
-the genome order of the import."""
+strings, the per-chromosome region index handed to the region counter, the
+genome order of the import, and the column index check of input matrices."""
 import gzip
 
 import numpy as np
@@ -109,3 +109,17 @@ def test_sorted_chrom_sizes_byte_order():
     with pytest.raises(ValueError):
         ChromSizes([("a", 1), ("a", 2)])
     assert np.asarray(sorted_chrom_sizes(d).sizes).sum() == sum(d.values())
+
+
+def test_column_index_check():
+    """Matrices with a column index outside [0, m) are refused before any
+    kernel looks the column up (SciPy does not check bounds by default)."""
+    from snapatac2_gb300._binning import DeviceCSR
+    from snapatac2_gb300._eigen import check_column_indices
+    ptr = torch.tensor([0, 2, 3], dtype=torch.int64)
+    check_column_indices(DeviceCSR(ptr, torch.tensor([0, 4, 1], dtype=torch.int32), None, (2, 5)))
+    check_column_indices(DeviceCSR(torch.zeros(2, dtype=torch.int64), torch.zeros(0, dtype=torch.int32), None,
+                                   (1, 5)))
+    for bad in ([0, 5, 1], [0, -1, 1]):
+        with pytest.raises(ValueError, match="column indices"):
+            check_column_indices(DeviceCSR(ptr, torch.tensor(bad, dtype=torch.int32), None, (2, 5)))
