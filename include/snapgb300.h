@@ -275,7 +275,8 @@ int sg_col_counts(int64_t nnz, int64_t m, const int32_t* indices, const uint32_t
 
 /* Keep the entries whose column maps to colmap[col] >= 0, renumbered to     */
 /* colmap[col] (X[:, selected_features], embedding.rs:36-41).  out_indices /  */
-/* out_values need capacity nnz(input); out_indptr[n] = kept nnz.            */
+/* out_values need capacity nnz(input); out_indptr[n] = kept nnz.  Column    */
+/* indices are not checked: each must index colmap (caller's check).        */
 int sg_csr_select_cols(int64_t n, const int64_t* indptr, const int32_t* indices, const float* values,
                        const int32_t* colmap, int64_t* out_indptr, int32_t* out_indices, float* out_values,
                        void* scan_scratch, void* stream);
@@ -337,6 +338,7 @@ int sg_idf_from_counts(int64_t n, int64_t m, const double* counts, double* w, un
 
 /* rinv[i] = 1 / ||x_i ⊙ w||_2 over the CSR rows (normalize, embedding.rs:  */
 /* 315-326); a row with no weight sets SG_ERR_NUMERIC with its index.        */
+/* Column indices are not checked: each must index w (caller's check).       */
 int sg_csr_row_norms(int64_t n, const int64_t* indptr, const int32_t* indices, const float* values,
                      const double* w, double* rinv, int* status, unsigned long long* bad, void* stream);
 
