@@ -9,5 +9,9 @@ package imports this package.
 * ``spectral`` -- IDF weights, row normalisation, degree, ARPACK ``eigsh``
 * ``knn``      -- exact kNN graph, C (OpenMP) brute force in FP64
 * ``features`` -- ``select_features`` ranking
+* ``fragments`` -- ``import_fragments``, Python + C
+* ``regions``  -- cell-by-region counts (peak matrix), Python + C (OpenMP)
+* ``genes``    -- annotation reading, promoter regions, gene-level maximum
+* ``nystrom``  -- Nyström extension and ``orthogonalize``
 """
 from ._build import build_oracle, load_lib  # noqa: F401

@@ -97,3 +97,65 @@ def region_counts(indptr, pos, length, chrom_names, chrom_sizes, peaks, *, strat
     names = [f"{c}:{s}-{e}" for c, s, e in regions]
     return (np.array(out_ptr, dtype=np.int64), np.array(out_idx, dtype=np.int64),
             np.array(out_val, dtype=np.uint32), names)
+
+
+_STRATEGY_CODES = {"insertion": 0, "fragment": 1, "paired-insertion": 2}
+
+
+def region_counts_c(indptr, pos, length, chrom_names, chrom_sizes, peaks, *, strategy="paired-insertion",
+                    paired=True, min_frag_size=None, max_frag_size=None, n_threads: int = 0, timing=None):
+    """``region_counts`` through oracle/regions.c (OpenMP over cells; same
+    result tuple).  Regions on chromosomes outside the genome stay features
+    that no fragment hits.  ``timing`` (a dict) receives ``count_s``, the
+    seconds of the two counting passes without the region index set-up."""
+    import ctypes
+    import time
+    from ._build import load_lib
+    lib = load_lib("regions")
+    f = lib.oracle_region_counts
+    P, I64 = ctypes.c_void_p, ctypes.c_int64
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_int, I64, P, P, P, ctypes.c_int, P, P, P, P, P, P, ctypes.c_int, I64, I64, ctypes.c_int,
+                  P, P, P, P]
+    regions = unique_regions(peaks)
+    cid = {c: i for i, c in enumerate(chrom_names)}
+    rows = sorted((cid[c], s, e, k) for k, (c, s, e) in enumerate(regions) if c in cid)
+    nc = len(chrom_names)
+    a = np.array(rows, dtype=np.int64).reshape(-1, 4)
+    rptr = np.zeros(nc + 1, dtype=np.int64)
+    np.cumsum(np.bincount(a[:, 0], minlength=nc), out=rptr[1:])
+    rstart, rend, rid = (np.ascontiguousarray(a[:, i]) for i in (1, 2, 3))
+    rmax = rend.copy()
+    for c in range(nc):
+        if rptr[c + 1] > rptr[c]:
+            rmax[rptr[c]:rptr[c + 1]] = np.maximum.accumulate(rend[rptr[c]:rptr[c + 1]])
+    cstart = np.concatenate([[0], np.cumsum(np.asarray(chrom_sizes, dtype=np.uint64))]).astype(np.uint64)
+    indptr = np.ascontiguousarray(indptr, dtype=np.int64)
+    pos = np.ascontiguousarray(pos, dtype=np.uint64)
+    n = indptr.size - 1
+    code = _STRATEGY_CODES[strategy] if paired else 3
+    ln = np.ascontiguousarray(length, dtype=np.uint32) if paired else None
+    mn = -1 if min_frag_size is None else int(min_frag_size)
+    mx = -1 if max_frag_size is None else int(max_frag_size)
+    out_ptr = np.zeros(n + 1, dtype=np.int64)
+    bad = ctypes.c_int64(-1)
+    ptrs = lambda x: None if x is None else x.ctypes.data  # noqa: E731
+    args = [n, ptrs(indptr), ptrs(pos), ptrs(ln), nc, ptrs(cstart), ptrs(rptr), ptrs(rstart), ptrs(rend), ptrs(rmax),
+            ptrs(rid), code, mn, mx, int(n_threads)]
+    t0 = time.perf_counter()
+    err = f(0, *args, ptrs(out_ptr), None, None, ctypes.byref(bad))
+    if err == 2:
+        raise ValueError(f"position {int(pos[bad.value])} outside the genome (fragment {bad.value})")
+    if err:
+        raise RuntimeError(f"oracle_region_counts failed ({err})")
+    np.cumsum(out_ptr, out=out_ptr)
+    out_idx = np.empty(max(int(out_ptr[-1]), 1), dtype=np.int64)
+    out_val = np.empty(max(int(out_ptr[-1]), 1), dtype=np.uint32)
+    err = f(1, *args, ptrs(out_ptr), ptrs(out_idx), ptrs(out_val), ctypes.byref(bad))
+    if err:
+        raise RuntimeError(f"oracle_region_counts failed ({err})")
+    if timing is not None:
+        timing["count_s"] = time.perf_counter() - t0
+    nnz = int(out_ptr[-1])
+    names = [f"{c}:{s}-{e}" for c, s, e in regions]
+    return out_ptr, out_idx[:nnz], out_val[:nnz], names

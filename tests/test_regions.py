@@ -1,4 +1,5 @@
-"""snap.pp.make_peak_matrix: the oracle on hand-made rows (CPU), the GPU
+"""snap.pp.make_peak_matrix: the oracle on hand-made rows and its C
+restatement against its Python one (CPU), the GPU
 region counter against the oracle (GPU), and a property that ties it to the
 tile matrix: with every genome tile given as a peak, the peak matrix is the
 tile matrix."""
@@ -31,6 +32,24 @@ def test_oracle_strategies():
     assert dict(zip(ix.tolist(), dv.tolist())) == {0: 1, 2: 1, 4: 1}
 
 
+def test_c_oracle_hand_made_rows():
+    ptr, pos, ln = [0, 1], [100], [200]
+    peaks = ["chr1:50-150", "chr1:250-400", "chr1:0-1000", "chr1:150-250", "chr2:0-10", "chr1:50-150"]
+    for strategy, kw in [("insertion", {}), ("paired-insertion", {}), ("fragment", {}),
+                         ("fragment", dict(max_frag_size=150))]:
+        got = org.region_counts_c(ptr, pos, ln, NAMES, SIZES, peaks, strategy=strategy, **kw)
+        ref = org.region_counts(ptr, pos, ln, NAMES, SIZES, peaks, strategy=strategy, **kw)
+        for g, r in zip(got[:3], ref[:3]):
+            np.testing.assert_array_equal(g, r)
+        assert got[3] == ref[3]
+    got = org.region_counts_c([0, 2], [100, 1005], [10, 3], NAMES, SIZES, peaks, paired=False)
+    assert dict(zip(got[1].tolist(), got[2].tolist())) == {0: 1, 2: 1, 4: 1}
+    with pytest.raises(ValueError, match="outside the genome"):
+        org.region_counts_c([0, 2], [100, 1500], [10, 3], NAMES, SIZES, peaks)
+    with pytest.raises(ValueError, match="outside the genome"):
+        org.region_counts([0, 2], [100, 1500], [10, 3], NAMES, SIZES, peaks)
+
+
 def _data(n_cells=30, seed=0):
     from snapatac2_gb300 import synthetic as S
     g = S.make_genome(total=8_000_000, n_chrom=6)
@@ -44,6 +63,25 @@ def _data(n_cells=30, seed=0):
     peaks += peaks[:7] + ["chrUn:0-100", f"{g[0][0]}:10-10", f"{g[1][0]}:0-{g[1][1]}"]
     rng.shuffle(peaks)
     return g, fr, peaks
+
+
+@pytest.mark.parametrize("strategy,kw", [("insertion", {}), ("paired-insertion", {}), ("fragment", {}),
+                                         ("paired-insertion", dict(min_frag_size=50, max_frag_size=300)),
+                                         ("single", {})])
+def test_c_oracle_matches_python_oracle(strategy, kw):
+    """The C restatement (OpenMP over cells) gives the Python restatement's
+    matrix bit for bit, whatever the thread count."""
+    g, fr, peaks = _data(seed=21 + len(kw))
+    names, sizes = [c for c, _ in g], [s for _, s in g]
+    paired = strategy != "single"
+    ref = org.region_counts(fr.indptr, fr.pos, fr.length, names, sizes, peaks, strategy=strategy, paired=paired,
+                            **kw)
+    for threads in (1, 4):
+        got = org.region_counts_c(fr.indptr, fr.pos, fr.length, names, sizes, peaks, strategy=strategy,
+                                  paired=paired, n_threads=threads, **kw)
+        for a, b in zip(got[:3], ref[:3]):
+            np.testing.assert_array_equal(a, b)
+        assert got[3] == ref[3]
 
 
 @pytest.mark.gpu
