@@ -103,11 +103,11 @@ int oracle_region_counts(int pass, int64_t n_cells, const int64_t *indptr, const
   int err = ORC_OK;
   int64_t first_bad = INT64_MAX;
 #ifdef _OPENMP
-  if (n_threads > 0) omp_set_num_threads(n_threads);
+  const int nt = n_threads > 0 ? n_threads : omp_get_max_threads();
 #else
   (void)n_threads;
 #endif
-#pragma omp parallel
+#pragma omp parallel num_threads(nt)
   {
     Vec h = {0, 0, 0}, q1 = {0, 0, 0}, q2 = {0, 0, 0};
     int local_err = ORC_OK;
