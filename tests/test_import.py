@@ -174,6 +174,24 @@ def test_gpu_import_errors():
             _import.import_text(_text(lines), GENOME, min_num_fragments=0, **kw)
 
 
+def test_c_oracle_roundtrip():
+    """test_tools.py:127-141 on the oracle (CPU): the imported fragments,
+    exported back to records, are the file's records."""
+    text, genome = _synthetic(n_cells=30, order="position", seed=21)
+    res = ofr.import_fragments_c(text, genome, min_num_fragments=0, sorted_by_barcode=False)
+    names, sizes = res["chrom_names"], res["chrom_sizes"]
+    starts = np.concatenate([[0], np.cumsum(sizes)[:-1]])
+    got = []
+    for r, bc in enumerate(res["obs_names"]):
+        lo, hi = res["indptr"][r], res["indptr"][r + 1]
+        for p, v in zip(res["indices"][lo:hi], res["data"][lo:hi]):
+            c = int(np.searchsorted(starts, p, side="right") - 1)
+            got.append((names[c], int(p - starts[c]), int(p - starts[c] + v), bc))
+    want = [tuple(f[:1]) + (int(f[1]), int(f[2]), f[3]) for f in
+            (ln.split("\t") for ln in text.decode().splitlines() if not ln.startswith("#"))]
+    assert len(got) > 1000 and sorted(got) == sorted(want)
+
+
 @pytest.mark.gpu
 def test_gpu_import_roundtrip_and_exclude():
     """test_tools.py:127-141 and test_pipeline.py:10-31 on a synthetic file."""
