@@ -185,10 +185,6 @@ def ptr(t: torch.Tensor | None) -> int | None:
     return t.data_ptr()
 
 
-def stream_handle(device: torch.device | None = None) -> int:
-    return torch.cuda.current_stream(device).cuda_stream
-
-
 class DeviceStatus:
     """Device-side status word + lowest offending index (see the C header)."""
 
