@@ -209,7 +209,7 @@ brinv_kernel(int64_t nrows, const int64_t* __restrict__ roff, int D, const int* 
   const int lane = threadIdx.x & 31;
   const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  if (B <= 8) {  // thread per row: W[i,:] <- W[i,:] Rinv, column c over k = 0..c in order
+  if constexpr (B <= 8) {  // thread per row: W[i,:] <- W[i,:] Rinv, column c over k = 0..c in order
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nrows;
          i += (int64_t)gridDim.x * blockDim.x) {
       const int d = find_ds(roff_s, D, i);
@@ -228,20 +228,20 @@ brinv_kernel(int64_t nrows, const int64_t* __restrict__ roff, int D, const int* 
 #pragma unroll
       for (int c = 0; c < B; ++c) W[i * B + c] = o[c];
     }
-    return;
-  }
-  for (int64_t i = gw; i < nrows; i += nw) {
-    const int d = find_ds(roff_s, D, i);
-    if (active && !active[d]) continue;
-    const double* ri = Rinv + (int64_t)d * B * B;
-    const T w = lane < B ? W[i * B + lane] : T(0);
-    T s = T(0);
+  } else {  // warp per row, lane c computes column c
+    for (int64_t i = gw; i < nrows; i += nw) {
+      const int d = find_ds(roff_s, D, i);
+      if (active && !active[d]) continue;
+      const double* ri = Rinv + (int64_t)d * B * B;
+      const T w = lane < B ? W[i * B + lane] : T(0);
+      T s = T(0);
 #pragma unroll
-    for (int k = 0; k < B; ++k) {
-      const T wk = __shfl_sync(0xffffffffu, w, k);
-      if (lane < B && k <= lane) s = fma(wk, (T)ri[k * B + lane], s);
+      for (int k = 0; k < B; ++k) {
+        const T wk = __shfl_sync(0xffffffffu, w, k);
+        if (lane < B && k <= lane) s = fma(wk, (T)ri[k * B + lane], s);
+      }
+      if (lane < B) W[i * B + lane] = s;
     }
-    if (lane < B) W[i * B + lane] = s;
   }
 }
 
