@@ -37,13 +37,32 @@ def _open(path):
 
 
 def _attrs_gtf(s: str) -> dict:
-    out = {}
-    for part in s.strip().split(";"):
-        part = part.strip()
-        if not part:
-            continue
-        k, _, v = part.partition(" ")
-        out.setdefault(k, v.strip().strip('"'))
+    """GTF attributes ``key value; key "value"; ...``: a quoted value may hold
+    ';' (the noodles GTF reader's entry format); the first of repeated keys
+    is kept."""
+    out: dict = {}
+    i, n = 0, len(s)
+    while i < n:
+        while i < n and s[i] in " \t;":
+            i += 1
+        if i >= n:
+            break
+        j = i
+        while j < n and s[j] not in " \t;":
+            j += 1
+        key = s[i:j]
+        while j < n and s[j] in " \t":
+            j += 1
+        if j < n and s[j] == '"':
+            k = s.find('"', j + 1)
+            k = n if k < 0 else k
+            val, j = s[j + 1:k], k + 1
+        else:
+            k = s.find(";", j)
+            k = n if k < 0 else k
+            val, j = s[j:k].strip(), k
+        out.setdefault(key, val)
+        i = j
     return out
 
 

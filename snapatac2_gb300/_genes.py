@@ -30,17 +30,44 @@ def _open(path):
 
 
 def _attrs(s: str, gff: bool) -> dict:
+    if not gff:
+        return _attrs_gtf(s)
     out: dict = {}
     for part in s.strip().split(";"):
         part = part.strip()
-        if not part:
-            continue
-        if gff:
+        if part:
             k, _, v = part.partition("=")
             out.setdefault(unquote(k.strip()), unquote(v.strip()))
+    return out
+
+
+def _attrs_gtf(s: str) -> dict:
+    """GTF attributes ``key value; key "value"; ...``: a quoted value may hold
+    ';' (the noodles GTF reader's entry format); the first of repeated keys
+    is kept."""
+    out: dict = {}
+    i, n = 0, len(s)
+    while i < n:
+        while i < n and s[i] in " \t;":
+            i += 1
+        if i >= n:
+            break
+        j = i
+        while j < n and s[j] not in " \t;":
+            j += 1
+        key = s[i:j]
+        while j < n and s[j] in " \t":
+            j += 1
+        if j < n and s[j] == '"':
+            k = s.find('"', j + 1)
+            k = n if k < 0 else k
+            val, j = s[j + 1:k], k + 1
         else:
-            k, _, v = part.partition(" ")
-            out.setdefault(k, v.strip().strip('"'))
+            k = s.find(";", j)
+            k = n if k < 0 else k
+            val, j = s[j:k].strip(), k
+        out.setdefault(key, val)
+        i = j
     return out
 
 

@@ -123,3 +123,28 @@ def test_column_index_check():
     for bad in ([0, 5, 1], [0, -1, 1]):
         with pytest.raises(ValueError, match="column indices"):
             check_column_indices(DeviceCSR(ptr, torch.tensor(bad, dtype=torch.int32), None, (2, 5)))
+
+
+def test_read_transcripts_reference_known_answer(tmp_path):
+    """The reference's test_read_transcript (genome.rs:599-643, via
+    tests/golden/transcripts.json): the same transcript from its GFF3 and GTF
+    text, and a GTF line whose quoted value holds ';' parses."""
+    import json
+    import os
+    from snapatac2_gb300._genes import read_transcripts
+    with open(os.path.join(os.path.dirname(__file__), "golden", "transcripts.json")) as fh:
+        g = json.load(fh)
+    (tmp_path / "a.gff3").write_text(g["gff"] + "\n")
+    (tmp_path / "a.gtf").write_text(g["gtf"] + "\n")
+    (tmp_path / "w.gtf").write_text(g["worked"] + "\n")
+    for reader in (read_transcripts, ogn.read_transcripts):
+        for name in ("a.gff3", "a.gtf"):
+            t = reader(tmp_path / name)[0]
+            assert {k: t[k] for k in g["expected"]} == g["expected"], (reader, name)
+        w = reader(tmp_path / "w.gtf")
+        assert len(w) == 1 and w[0]["transcript_id"] == "XM_5" and w[0]["gene_name"] == "RGD"
+    (tmp_path / "q.gtf").write_text('chr1\tG\ttranscript\t5\t9\t.\t-\t.\tgene_id "G"; transcript_id "T;1"; '
+                                    'gene_name "A;B"; level 2\n')
+    for reader in (read_transcripts, ogn.read_transcripts):
+        t = reader(tmp_path / "q.gtf")[0]
+        assert (t["transcript_id"], t["gene_name"], t["gene_id"]) == ("T;1", "A;B", "G")
