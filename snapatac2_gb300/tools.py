@@ -9,9 +9,8 @@ and output slots ``uns['spectral_eigenvalue']`` (float64[k']) and
 from __future__ import annotations
 
 import threading
-from typing import Literal
-
 import warnings
+from typing import Literal
 
 import numpy as np
 import scipy.sparse as sp
@@ -201,11 +200,16 @@ def spectral(
     if distance_metric != "cosine":
         raise NotImplementedError("only distance_metric='cosine' (matrix-free) is supported")
     if sample_size < n_sample:
-        # Nyström (embedding.rs:61-131): landmark solve with random_state 0, as the reference
+        # Nyström (embedding.rs:61-131): landmark solve with random_state 0, and IDF weights: the
+        # reference's call (_embedding.py:264) passes neither random_state nor feature_weights
         from ._nystrom import spectral_nystrom
+        if feature_weights is not None:
+            warnings.warn("feature_weights are not used with sample_size (the reference's Nystrom call "
+                          "takes IDF weights); call snapatac2_gb300._nystrom.spectral_nystrom to weight "
+                          "the landmarks", stacklevel=2)
         evals, evecs = spectral_nystrom(adata.X, features, n_comps, sample_size,
                                         weighted_by_degree=sample_method != "random", chunk_size=chunk_size,
-                                        feature_weights=feature_weights, random_state=0, precision=precision,
+                                        feature_weights=None, random_state=0, precision=precision,
                                         block=block, device=device)
     else:
         if precision == "auto":

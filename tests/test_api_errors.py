@@ -72,3 +72,20 @@ def test_import_fragments_arguments(tmp_path):
         snap.pp.import_fragments(str(p), {})
     with pytest.raises(NotImplementedError, match="backed"):
         snap.pp.import_fragments(str(p), {"chr1": 1000}, file=str(tmp_path / "o.h5ad"))
+
+
+def test_spectral_nystrom_ignores_feature_weights_like_the_reference(monkeypatch):
+    """_embedding.py:264 calls the Nystrom path without feature_weights: the
+    weights are dropped (with a warning) and IDF is used."""
+    from snapatac2_gb300 import _nystrom
+    seen = {}
+
+    def fake(X, features, n_comps, sample_size, **kw):
+        seen.update(kw)
+        return np.array([0.5]), np.zeros((X.shape[0], 1))
+
+    monkeypatch.setattr(_nystrom, "spectral_nystrom", fake)
+    ad = _adata()
+    with pytest.warns(UserWarning, match="feature_weights are not used"):
+        snap.tl.spectral(ad, features=None, sample_size=10, feature_weights=np.ones(40))
+    assert seen["feature_weights"] is None and seen["random_state"] == 0
