@@ -219,7 +219,7 @@ def select_features(adata, n_features: int = 500000, filter_lower_quantile: floa
         return None if inplace else res
     if whitelist is not None or blacklist is not None:
         raise NotImplementedError("whitelist/blacklist BED filtering is not supported")
-    if max_iter != 1:
+    if max_iter > 1:  # the reference iterates while iter < max_iter, from 1 (_basic.py:1067-1068)
         raise NotImplementedError("iterative feature selection (max_iter > 1) is not supported")
     X = adata.X
     count = column_counts(X, device)
