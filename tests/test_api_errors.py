@@ -89,3 +89,8 @@ def test_spectral_nystrom_ignores_feature_weights_like_the_reference(monkeypatch
     with pytest.warns(UserWarning, match="feature_weights are not used"):
         snap.tl.spectral(ad, features=None, sample_size=10, feature_weights=np.ones(40))
     assert seen["feature_weights"] is None and seen["random_state"] == 0
+
+
+def test_spectral_needs_selected_features():
+    with pytest.raises(NameError, match="Please call `select_features` first"):
+        snap.tl.spectral(_adata())
