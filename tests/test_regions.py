@@ -142,3 +142,43 @@ def test_gpu_make_peak_matrix_api(tmp_path):
         snap.pp.make_peak_matrix(ad, peak_file=str(p), use_rep="peaks")
     assert snap.pp.make_peak_matrix(ad, inplace=True) is None
     assert (ad.X != b.X).nnz == 0
+
+
+def test_c_oracle_random_small_cases():
+    """Both restatements on 60 random tiny genomes: nested, touching and
+    zero-width peaks, repeats, fragments at chromosome edges, zero-length
+    fragments, random size filters, every strategy."""
+    rng = np.random.default_rng(123)
+    strategies = ["insertion", "fragment", "paired-insertion", "single"]
+    for trial in range(60):
+        sizes = [int(x) for x in rng.integers(50, 400, 3)]
+        names = ["chrA", "chrB", "chrC"]
+        peaks = []
+        for _ in range(int(rng.integers(1, 30))):
+            c = int(rng.integers(0, 4))
+            s = int(rng.integers(0, 420))
+            peaks.append(f"{(names + ['chrZ'])[c]}:{s}-{s + int(rng.integers(0, 120))}")
+        peaks += peaks[:3]
+        n_cells = int(rng.integers(1, 8))
+        counts = rng.integers(0, 25, n_cells)
+        indptr = np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
+        F = int(indptr[-1])
+        chrom = rng.integers(0, 3, F)
+        csz = np.asarray(sizes)[chrom]
+        length = rng.integers(0, 150, F)
+        length = np.minimum(length, csz)
+        start = (rng.random(F) * (csz - length + 1)).astype(np.int64)
+        base = np.concatenate([[0], np.cumsum(sizes)[:-1]])
+        pos = (base[chrom] + start).astype(np.uint64)
+        strategy = strategies[trial % 4]
+        kw = {}
+        if trial % 3 == 0:
+            kw = dict(min_frag_size=int(rng.integers(0, 60)), max_frag_size=int(rng.integers(60, 160)))
+        paired = strategy != "single"
+        if not paired:
+            kw = {}
+        ref = org.region_counts(indptr, pos, length, names, sizes, peaks, strategy=strategy, paired=paired, **kw)
+        got = org.region_counts_c(indptr, pos, length, names, sizes, peaks, strategy=strategy, paired=paired, **kw)
+        for a, b in zip(got[:3], ref[:3]):
+            np.testing.assert_array_equal(a, b, err_msg=f"trial {trial}")
+        assert got[3] == ref[3]
