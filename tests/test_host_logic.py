@@ -148,3 +148,28 @@ def test_read_transcripts_reference_known_answer(tmp_path):
     for reader in (read_transcripts, ogn.read_transcripts):
         t = reader(tmp_path / "q.gtf")[0]
         assert (t["transcript_id"], t["gene_name"], t["gene_id"]) == ("T;1", "A;B", "G")
+
+
+def test_import_result_to_anndata_slots(caplog):
+    """The import's AnnData layout (import.rs:161-210, genome.rs:247-251):
+    obsm['fragment_paired'] (uint32 sizes, genome-wide columns), obs QC
+    columns, uns['reference_sequences'], and the reference's warning with
+    no cells (import.rs:112)."""
+    import logging
+    from snapatac2_gb300._import import FRAGMENT_PAIRED, ImportResult, to_anndata
+    from snapatac2_gb300.genome import ChromSizes
+    cs = ChromSizes([("chr1", 100), ("chr2", 50)])
+    r = ImportResult(key=FRAGMENT_PAIRED, obs_names=["A", "B"], indptr=np.array([0, 1, 3]),
+                     indices=np.array([5, 10, 120]), data=np.array([20, 30, 10], dtype=np.uint32),
+                     n_fragment=np.array([1, 2], dtype=np.uint64), frac_dup=np.array([0.0, 0.5]),
+                     frac_mito=np.array([0.0, 0.0]), chrom_sizes=cs, info={})
+    ad = to_anndata(r)
+    m = ad.obsm[FRAGMENT_PAIRED]
+    assert m.shape == (2, 150) and m.dtype == np.uint32 and m.indices.tolist() == [5, 10, 120]
+    assert list(ad.obs_names) == ["A", "B"] and ad.n_obs == 2
+    assert set(ad.obs.keys()) == {"n_fragment", "frac_dup", "frac_mito"}
+    ref = ad.uns["reference_sequences"]
+    assert list(ref["reference_seq_name"]) == ["chr1", "chr2"] and list(ref["reference_seq_length"]) == [100, 50]
+    with caplog.at_level(logging.WARNING):
+        empty = to_anndata(ImportResult(None, [], None, None, None, None, None, None, cs, {}))
+    assert empty.n_obs == 0 and "No barcodes passed the QC filter. No data is imported." in caplog.text
