@@ -1,7 +1,7 @@
 """ORACLE -- test infrastructure only.
 
 CPU restatements of the reference's arithmetic on the cell-embedding path,
-used as the checker by ``tests/``, by ``__graft_entry__.smoke()`` and by the
+used for comparison by ``tests/``, by ``__graft_entry__.smoke()`` and by the
 CPU-baseline leg of ``bench.py``.  Nothing in the ``snapatac2_gb300``
 package imports this package.
 

@@ -1,5 +1,5 @@
 /*
- * ORACLE -- test infrastructure only (checker and CPU-baseline leg).
+ * ORACLE -- test infrastructure only (tests and the CPU-baseline leg).
  *
  * Exact Euclidean k-nearest-neighbour graph, restating
  *   snapatac2-core/src/utils/knn.rs:9-31  nearest_neighbour_graph

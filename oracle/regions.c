@@ -1,6 +1,6 @@
 /*
  * ORACLE -- test infrastructure only.  Tests and the CPU baseline leg of the
- * benchmark call this as the checker; the product path never does.
+ * benchmark compare results with it; the product path never calls it.
  *
  * Cell-by-region counts (the peak matrix over fragments) restated in C for
  * a compiled-speed CPU baseline; oracle/regions.py holds the loop-for-loop

@@ -1,7 +1,7 @@
 /*
  * ORACLE -- test infrastructure only.  Tests, the smoke check and the CPU
- * baseline leg of the benchmark call this as the checker; the product path
- * never does.
+ * baseline leg of the benchmark compare results with it; the product path
+ * never calls it.
  *
  * CPU restatement of the reference's tile binning:
  *   GenomeBaseIndex        snapatac2-core/src/genome.rs:288-406,419-434
