@@ -159,3 +159,41 @@ def region_counts_c(indptr, pos, length, chrom_names, chrom_sizes, peaks, *, str
     nnz = int(out_ptr[-1])
     names = [f"{c}:{s}-{e}" for c, s, e in regions]
     return out_ptr, out_idx[:nnz], out_val[:nnz], names
+
+
+def aggregate_x(X, var_names, chrom_names, peaks):
+    """``use_x=True`` of ``create_peak_matrix`` (snapatac2-core/src/feature_count/matrix.rs:121-128):
+    ``read_chrom_values().aggregate_by(RegionCounter)`` (data_iter.rs:866-891)
+    -- each entry (feature interval j, value v) of a cell's row adds v to
+    every region overlapping interval j (``RegionCounter::insert``,
+    counter.rs:95-106); rows sorted by region index.  Returns (indptr,
+    indices, data as float64, names)."""
+    import scipy.sparse as sp
+    X = sp.csr_matrix(X)
+    regions = unique_regions(peaks)
+    by_chrom: dict = {}
+    for k, (c, s, e) in enumerate(regions):
+        by_chrom.setdefault(c, []).append((s, e, k))
+    arrays = {c: (np.array([v[0] for v in lst], dtype=np.int64), np.array([v[1] for v in lst], dtype=np.int64),
+                  np.array([v[2] for v in lst], dtype=np.int64)) for c, lst in by_chrom.items()}
+    feat = [parse_region(str(v)) for v in var_names]
+    hit_of = []
+    for c, s, e in feat:
+        if c in arrays:
+            rs, re_, rk = arrays[c]
+            hit_of.append(sorted(rk[(rs < e) & (re_ > s)].tolist()))
+        else:
+            hit_of.append([])
+    out_ptr, out_idx, out_val = [0], [], []
+    for r in range(X.shape[0]):
+        acc: dict = {}
+        for j, v in zip(X.indices[X.indptr[r]:X.indptr[r + 1]], X.data[X.indptr[r]:X.indptr[r + 1]]):
+            for k in hit_of[int(j)]:
+                acc[k] = acc.get(k, 0.0) + float(v)
+        for k in sorted(acc):
+            out_idx.append(k)
+            out_val.append(acc[k])
+        out_ptr.append(len(out_idx))
+    names = [f"{c}:{s}-{e}" for c, s, e in regions]
+    return (np.array(out_ptr, dtype=np.int64), np.array(out_idx, dtype=np.int64),
+            np.array(out_val, dtype=np.float64), names)

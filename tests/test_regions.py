@@ -7,6 +7,7 @@ import gzip
 
 import numpy as np
 import pytest
+import scipy.sparse as sp
 
 from oracle import regions as org
 
@@ -182,3 +183,38 @@ def test_c_oracle_random_small_cases():
         for a, b in zip(got[:3], ref[:3]):
             np.testing.assert_array_equal(a, b, err_msg=f"trial {trial}")
         assert got[3] == ref[3]
+
+
+def test_oracle_aggregate_x_hand_made():
+    var = ["chr1:0-100", "chr1:100-200", "chr2:0-50", "chr9:0-10"]
+    X = np.array([[1, 2, 0, 5], [0, 0, 3, 0]], dtype=np.float64)
+    peaks = ["chr1:50-150", "chr1:150-160", "chr2:10-20", "chr1:0-1000"]
+    ip, ix, dv, names = org.aggregate_x(X, var, ["chr1", "chr2"], peaks)
+    assert names == peaks
+    assert ip.tolist() == [0, 3, 4]
+    assert dict(zip(ix[:3].tolist(), dv[:3].tolist())) == {0: 3.0, 1: 2.0, 3: 3.0}
+    assert ix[3:].tolist() == [2] and dv[3:].tolist() == [3.0]
+
+
+def test_oracle_aggregate_x_of_tiles_is_the_insertion_peak_matrix():
+    """Peaks made of whole 500 bp tiles: aggregating the insertion-count tile
+    matrix (use_x) gives the insertion-strategy peak matrix of the fragments,
+    since every insertion lies in exactly one tile."""
+    from oracle import binning as ob
+    g, fr, _ = _data(n_cells=12, seed=31)
+    names, sizes = [c for c, _ in g], [s for _, s in g]
+    ip, ix, dv, ncol = ob.tile_bin(fr.indptr, fr.pos, fr.length, g, bin_size=500,
+                                   counting_strategy="insertion", exclude_chroms=[])[:4]
+    tiles = [f"{c}:{s}-{min(s + 500, size)}" for c, size in g for s in range(0, size, 500)]
+    assert len(tiles) == ncol
+    rng = np.random.default_rng(2)
+    peaks = []
+    for c, size in g:
+        for s in np.sort(rng.choice(size // 500 - 4, 40, replace=False)).tolist():
+            peaks.append(f"{c}:{s * 500}-{(s + int(rng.integers(1, 4))) * 500}")
+    X = sp.csr_matrix((dv.astype(np.float64), ix, ip), shape=(fr.n_cells, ncol))
+    agg = org.aggregate_x(X, tiles, names, peaks)
+    ref = org.region_counts(fr.indptr, fr.pos, fr.length, names, sizes, peaks, strategy="insertion")
+    np.testing.assert_array_equal(agg[0], ref[0])
+    np.testing.assert_array_equal(agg[1], ref[1])
+    np.testing.assert_array_equal(agg[2], ref[2].astype(np.float64))
