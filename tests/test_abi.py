@@ -31,3 +31,10 @@ def test_python_signatures_cover_header(built_lib):
 def test_version_and_status(built_lib):
     assert built_lib.sg_version() >= 100
     assert built_lib.sg_status_string(2) == b"position out of range of the genome or chromosome"
+
+
+def test_integration_guide_indexes_every_entry_point():
+    """INTEGRATION.md's entry-point index names every declared function."""
+    doc = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    missing = [s for s in declared_symbols() if f"`{s}`" not in doc]
+    assert not missing, missing
