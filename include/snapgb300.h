@@ -170,7 +170,9 @@ int sg_frag_index_lines(const uint8_t* text, int64_t nbytes, const void* scratch
 /* line plus 32 B per whitelist entry).                                      */
 int64_t sg_frag_workspace_bytes(int64_t n_lines, int64_t n_whitelist);
 
-/* The import.  Chromosomes: n_chrom names sorted by bytes (chrom_blob +    */
+/* The import (import_fragments, snapatac2-core/src/preprocessing/          */
+/* import.rs:31-210, entered from preprocessing.rs:87-184 of the Python     */
+/* package).  Chromosomes: n_chrom names sorted by bytes (chrom_blob +      */
 /* chrom_off[n_chrom + 1]), their lengths, the cumulative length before each */
 /* (chrom_base) and a mitochondrial flag per name; genome_size = total.      */
 /* Whitelist (has_whitelist != 0): n_whitelist byte strings (wl_blob +       */
@@ -382,6 +384,8 @@ int sg_gather_ceiling(int dtype, int block, int64_t nnz, const int32_t* idx, con
                       void* stream);
 
 /* ---- block Krylov-Schur (thick-restart block Lanczos) building blocks --- */
+/* Together they replace the ARPACK eigsh call of eigen                      */
+/* (snapatac2-python/src/embedding.rs:155-188; ARPACK itself is SciPy's).    */
 /* Q: n x ldq row-major basis; W: n x block working block.                   */
 
 /* Number of per-CTA partials of the projections (part = parts*ncols*block). */
