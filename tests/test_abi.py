@@ -38,3 +38,44 @@ def test_integration_guide_indexes_every_entry_point():
     doc = open(os.path.join(ROOT, "INTEGRATION.md")).read()
     missing = [s for s in declared_symbols() if f"`{s}`" not in doc]
     assert not missing, missing
+
+
+def _declarations():
+    """name -> (return type, [parameter types]) from the header."""
+    src = open(os.path.join(ROOT, "include", "snapgb300.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    src = re.sub(r"#[^\n]*", "", src)
+    out = {}
+    for m in re.finditer(r"([\w\s\*]+?)\b(sg_\w+)\s*\(([^)]*)\)\s*;", src):
+        ret = " ".join(m.group(1).split())
+        params = [p.strip() for p in m.group(3).split(",")]
+        if params == ["void"] or params == [""]:
+            params = []
+        types = [re.sub(r"\s*\b\w+$", "", p) if "*" not in p.split()[-1] else p for p in params]
+        out[m.group(2)] = (ret, [" ".join(t.replace("*", " * ").split()) for t in types])
+    return out
+
+
+def _ctype_of(c_type: str):
+    import ctypes
+    if "*" in c_type:
+        return ctypes.c_void_p, ctypes.c_char_p
+    base = c_type.replace("const", "").strip()
+    table = {"int": ctypes.c_int, "int64_t": ctypes.c_int64, "uint32_t": ctypes.c_uint32,
+             "uint64_t": ctypes.c_uint64, "double": ctypes.c_double}
+    return (table[base],)
+
+
+def test_python_signatures_match_header_arguments():
+    """Every ctypes binding has the header's argument count and compatible
+    types (pointers as void* / char*, integers and doubles of the same width),
+    and the same return type."""
+    from snapatac2_gb300 import _lib
+    decl = _declarations()
+    assert set(decl) == set(declared_symbols())
+    for name, (ret, params) in decl.items():
+        res, args = _lib.SIGNATURES[name]
+        assert len(args) == len(params), (name, len(args), len(params))
+        for i, (c, py) in enumerate(zip(params, args)):
+            assert py in _ctype_of(c), (name, i, c, py)
+        assert res in _ctype_of(ret.replace("const char *", "char *").replace("const char*", "char *")), (name, ret)
