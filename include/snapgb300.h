@@ -497,9 +497,11 @@ int sg_square_values(int64_t nnz, const float* values, float* out, void* stream)
 /* memory: the scratch is a fixed array inside the library (about 33 MB per  */
 /* GPU that loads it, held until exit).  Limits: n <= 16384 points,          */
 /* d <= 32, k <= 100 (k + margin is capped at 128); larger problems return   */
-/* SG_ERR_CAP without touching the outputs.  The first call on a device      */
-/* looks up the array's device address (cudaGetSymbolAddress, with that      */
-/* device current), so make that first call before any stream capture.      */
+/* SG_ERR_CAP without touching the outputs.  Every call looks up the array's */
+/* device address (cudaGetSymbolAddress, with the caller's device current),  */
+/* so the address stays right after cudaDeviceReset; the first call on a    */
+/* device also loads the library's device code there (lazy module loading),  */
+/* so make that first call before any stream capture.                        */
 /* All calls share the one array: calls that overlap on the GPU (different   */
 /* streams, no ordering between them) race and must be avoided.             */
 int sg_knn_noalloc(const double* X, int64_t n, int d, int k, int margin, int64_t* nbr, double* dist,

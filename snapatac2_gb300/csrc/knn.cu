@@ -480,6 +480,7 @@ struct TcSmem {
   uint64_t mdone[2];        // accumulator buffer x holds tile k (commit)
   uint64_t tfree[2];        // accumulator buffer x read by the 4 consumer warps
   uint64_t aful;            // query operands landed
+  uint64_t drain;           // failure path: every MMA issued so far has completed (commit)
   uint32_t tmem_slot;
   int failed;
   __align__(128) unsigned char A[2 * kTMat];
@@ -492,6 +493,8 @@ struct TcSmem {
   unsigned queue[kTConsumers][kTQueue];
   int nqueue[kTConsumers];
 };
+
+static_assert(sizeof(TcSmem) <= 232448, "tensor-core filter shared memory above the per-CTA limit");
 
 __device__ __forceinline__ uint32_t tc_off(int r, int t) {
   return (uint32_t)((r >> 3) * 512 + (t >> 3) * 128 + (r & 7) * 16 + (t & 7) * 2);
@@ -542,6 +545,7 @@ tc_filter_kernel(const float* __restrict__ XT, const unsigned char* __restrict__
       mbar_init(&sm.tfree[x], kTConsumers);
     }
     mbar_init(&sm.aful, 1);
+    mbar_init(&sm.drain, 1);
     sm.failed = 0;
     fence_barrier_init();
   }
@@ -564,15 +568,19 @@ tc_filter_kernel(const float* __restrict__ XT, const unsigned char* __restrict__
   if (wid == kTConsumers) {
     // ---------------- producer: tile copies and MMAs (one thread) ---------
     if (lane == 0) {
+      // tiles [waited, issued) have copies in flight, at most one per buffer
+      int64_t issued = 0, waited = 0;
       auto issue = [&](int64_t k) {
         const int b = (int)(k % kTBuf);
         mbar_expect_tx(&sm.full[b], kTTile);
         bulk_copy(sm.Bt[b], TC + k * kTTile, kTTile, &sm.full[b]);
+        issued = k + 1;
       };
       mbar_expect_tx(&sm.aful, 2 * kTMat);
       bulk_copy(sm.A, TC + (qbase / kFC) * kTTile, 2 * kTMat, &sm.aful);
       for (int64_t k = 0; k < kTBuf && k < ntiles; ++k) issue(k);
-      bool ok = mbar_wait(&sm.aful, 0);
+      const bool a_ok = mbar_wait(&sm.aful, 0);
+      bool ok = a_ok;
       const uint32_t a_hi = smem_u32(sm.A), a_lo = a_hi + kTMat;
       // tile k: MMA as soon as it landed and its accumulator buffer was read
       // out (tile k - 2); then refill the buffer tile k - 1 used with tile
@@ -581,6 +589,7 @@ tc_filter_kernel(const float* __restrict__ XT, const unsigned char* __restrict__
       for (int64_t k = 0; ok && k < ntiles; ++k) {
         const int b = (int)(k % kTBuf), x = (int)(k & 1);
         ok = mbar_wait(&sm.full[b], (uint32_t)((k / kTBuf) & 1));
+        if (ok) waited = k + 1;
         if (ok && k >= 2) ok = mbar_wait(&sm.tfree[x], (uint32_t)(((k / 2) - 1) & 1));
         if (!ok) break;
         tc_fence_after();
@@ -603,7 +612,18 @@ tc_filter_kernel(const float* __restrict__ XT, const unsigned char* __restrict__
           issue(kt);
         }
       }
-      if (!ok) atomicExch(&sm.failed, 1);
+      if (!ok) {
+        atomicExch(&sm.failed, 1);
+        // before the CTA frees TMEM and exits, let what is in flight land:
+        // the query copy, every tile copy not yet waited for (one phase per
+        // buffer, so each parity wait is unambiguous) and every committed
+        // MMA (a last commit completes once all earlier ones have); each
+        // wait is bounded like the others
+        if (!a_ok) mbar_wait(&sm.aful, 0);
+        for (int64_t t = waited; t < issued; ++t) mbar_wait(&sm.full[t % kTBuf], (uint32_t)((t / kTBuf) & 1));
+        umma_commit(&sm.drain);
+        mbar_wait(&sm.drain, 0);
+      }
     }
   } else {
     // ---------------- consumers: filter from TMEM, verify, lists ----------
@@ -908,35 +928,54 @@ struct KnnScratch {
   int64_t bytes;
 };
 
-inline int64_t align256(int64_t x) { return (x + 255) / 256 * 256; }
+constexpr int64_t align256(int64_t x) { return (x + 255) / 256 * 256; }
+
+// Byte offsets of the scratch regions (each 256-byte aligned) and the total;
+// constexpr so that the allocation-free entry point can size its fixed array
+// from the same arithmetic.
+struct KnnOffsets {
+  int64_t mp, mean, XT, nrm, TC, X64, cand, tau, flagged, fcand, fcand_d, counters, bytes;
+};
+
+constexpr KnnOffsets knn_offsets(int64_t n, int DP, int k, int Kp) {
+  KnnOffsets o{};
+  int64_t at = 0;
+  const int64_t npad = (n + kFC - 1) / kFC * kFC;
+  o.mp = at; at += align256((int64_t)kMeanParts * 64 * 8);
+  o.mean = at; at += align256(64 * 8);
+  o.XT = at; at += align256(npad * DP * 4);
+  o.nrm = at; at += align256(npad * 4);
+  o.TC = at; at += DP == 32 ? align256(npad / kFC * kTTile) : 0;
+  o.X64 = at; at += align256(n * DP * 8);
+  o.cand = at; at += align256(n * (int64_t)Kp * 4);
+  o.tau = at; at += align256(n * 4);
+  o.flagged = at; at += align256(n * 4);
+  o.fcand = at; at += align256(n * (int64_t)k * 4);
+  o.fcand_d = at; at += align256(n * (int64_t)k * 8);
+  o.counters = at; at += align256(16);
+  o.bytes = at;
+  return o;
+}
 
 KnnScratch knn_layout(char* base, int64_t n, int DP, int k, int Kp) {
+  const KnnOffsets o = knn_offsets(n, DP, k, Kp);
   KnnScratch s{};
-  int64_t o = 0;
-  auto take = [&](int64_t b) { int64_t r = o; o += align256(b); return r; };
-  const int64_t npad = (n + kFC - 1) / kFC * kFC;
-  const int64_t omp = take((int64_t)kMeanParts * 64 * 8), omean = take(64 * 8);
-  const int64_t oXT = take(npad * DP * 4), onrm = take(npad * 4),
-                oTC = DP == 32 ? take(npad / kFC * kTTile) : 0, oX64 = take(n * DP * 8),
-                oc = take(n * (int64_t)Kp * 4),
-                ot = take(n * 4), of = take(n * 4), ofc = take(n * (int64_t)k * 4),
-                ofd = take(n * (int64_t)k * 8), on = take(16);
   if (base) {
-    s.mpart = (double*)(base + omp);
-    s.mean = (double*)(base + omean);
-    s.XT = (float*)(base + oXT);
-    s.nrm = (float*)(base + onrm);
-    s.TC = DP == 32 ? (unsigned char*)(base + oTC) : nullptr;
-    s.X64 = (double*)(base + oX64);
-    s.cand = (int*)(base + oc);
-    s.tau32 = (float*)(base + ot);
-    s.flagged = (int*)(base + of);
-    s.fcand = (int*)(base + ofc);
-    s.fcand_d = (double*)(base + ofd);
-    s.nflag = (int*)(base + on);
-    s.maxnorm = (unsigned*)(base + on + 8);
+    s.mpart = (double*)(base + o.mp);
+    s.mean = (double*)(base + o.mean);
+    s.XT = (float*)(base + o.XT);
+    s.nrm = (float*)(base + o.nrm);
+    s.TC = DP == 32 ? (unsigned char*)(base + o.TC) : nullptr;
+    s.X64 = (double*)(base + o.X64);
+    s.cand = (int*)(base + o.cand);
+    s.tau32 = (float*)(base + o.tau);
+    s.flagged = (int*)(base + o.flagged);
+    s.fcand = (int*)(base + o.fcand);
+    s.fcand_d = (double*)(base + o.fcand_d);
+    s.nflag = (int*)(base + o.counters);
+    s.maxnorm = (unsigned*)(base + o.counters + 8);
   }
-  s.bytes = o;
+  s.bytes = o.bytes;
   return s;
 }
 
@@ -1065,46 +1104,32 @@ extern "C" int sg_knn(const double* X, int64_t n, int d, int k, int margin, int6
 // of this library's device image: every GPU that loads the library holds it
 // (about 33 MB) until the process exits.
 // ---------------------------------------------------------------------------
-#include <mutex>
-
 namespace sg {
 namespace {
 
 constexpr int64_t kNoAllocMaxN = 16384;  // points
 constexpr int kNoAllocMaxDim = 32;       // dimensions
 constexpr int kNoAllocMaxK = 100;        // neighbours
-constexpr int64_t kA256(int64_t x) { return (x + 255) / 256 * 256; }
-// knn_layout(kNoAllocMaxN, 32, kNoAllocMaxK, kMaxKp) written out (kNoAllocMaxN is
-// a multiple of the 128-point tile): mean partials, mean, tile-transposed
-// FP32 points, their norms, tensor-core operand tiles, X64, candidates, tau,
-// flagged, fallback candidates and distances, counters
+// sized by the scratch layout of the largest accepted problem: 16,384
+// points (whole 128-point tiles), 32 dimensions (the tensor-core operand
+// tiles are included), k = 100, candidate lists of kMaxKp
 static_assert(kNoAllocMaxN % kFC == 0, "no-alloc capacity must be whole tiles");
-constexpr int64_t kNoAllocBytes =
-    kA256((int64_t)kMeanParts * 64 * 8) + kA256(64 * 8) + kA256(kNoAllocMaxN * kNoAllocMaxDim * 4) +
-    kA256(kNoAllocMaxN * 4) + kA256(kNoAllocMaxN / kFC * kTTile) + kA256(kNoAllocMaxN * kNoAllocMaxDim * 8) +
-    kA256(kNoAllocMaxN * kMaxKp * 4) + kA256(kNoAllocMaxN * 4) + kA256(kNoAllocMaxN * 4) +
-    kA256(kNoAllocMaxN * kNoAllocMaxK * 4) + kA256(kNoAllocMaxN * kNoAllocMaxK * 8) + kA256(16);
+constexpr int64_t kNoAllocBytes = knn_offsets(kNoAllocMaxN, kNoAllocMaxDim, kNoAllocMaxK, kMaxKp).bytes;
 
 static __device__ __align__(256) unsigned char g_knn_scratch[kNoAllocBytes];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_knn_scratch_mu;
-void* g_knn_scratch_ptr[kMaxDevices] = {};
-
 // Device address of g_knn_scratch on the current device.  In host code the
 // name g_knn_scratch is only a host-side stand-in, so the address is looked
-// up once per device (with that device current) and kept.
+// up with the device current and the return code checked.  The lookup is
+// repeated on every call (it is a table lookup in the CUDA runtime): a cached
+// address would go stale when the device's context is destroyed and made
+// again (cudaDeviceReset), which reloads the module at a new address.  The
+// first lookup on a device loads the module that holds the array (CUDA's
+// lazy module loading).
 int knn_scratch_address(void** out) {
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess) return SG_ERR_CUDA;
-  if (dev < 0 || dev >= kMaxDevices) return SG_ERR_ARG;
-  std::lock_guard<std::mutex> lock(g_knn_scratch_mu);
-  if (!g_knn_scratch_ptr[dev]) {
-    void* p = nullptr;
-    if (cudaGetSymbolAddress(&p, g_knn_scratch) != cudaSuccess || !p) return SG_ERR_CUDA;
-    g_knn_scratch_ptr[dev] = p;
-  }
-  *out = g_knn_scratch_ptr[dev];
+  void* p = nullptr;
+  if (cudaGetSymbolAddress(&p, g_knn_scratch) != cudaSuccess || !p) return SG_ERR_CUDA;
+  *out = p;
   return SG_OK;
 }
 
