@@ -7,7 +7,8 @@ import subprocess
 import threading
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
-_SOURCES = {"tilebin": "tile_bin.c", "knn": "knn.c", "fragments": "fragments.c", "regions": "regions.c"}
+_SOURCES = {"tilebin": "tile_bin.c", "knn": "knn.c", "fragments": "fragments.c", "regions": "regions.c",
+            "gram": "gram.c"}
 _LOCK = threading.Lock()
 _LIBS: dict[str, ctypes.CDLL] = {}
 

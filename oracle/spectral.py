@@ -10,6 +10,8 @@ FP64 restatement of the reference's matrix-free cosine spectral embedding:
                    operator v -> X (Xᵀ v) - D v with ``v0 = rand(n)`` after
                    ``numpy.random.seed(seed)``; this module makes the same call
                    on the installed SciPy, so the arithmetic is the reference's.
+  ``threaded=True`` evaluates the same operator with an OpenMP C matvec
+                   (``gram.c``) for sizes where SciPy's would take minutes.
 * ``spectral``     ``snapatac2-python/python/snapatac2/tools/_embedding.py:223-293``
                    (n_comps clamp, ``weighted_by_sd`` filter and scaling).
 """
@@ -53,13 +55,48 @@ def degree_scale(Xn: sp.csr_matrix):
     return sp.csr_matrix(Xs), dinv
 
 
-def eigen(X: sp.csr_matrix, D: np.ndarray, k: int, seed: int):
-    """Same ``eigsh`` call as the reference's embedded ``eigen`` function."""
+def _threaded_matvec(X: sp.csr_matrix, D: np.ndarray):
+    """f(v) = X (Xᵀ v) - D v by the OpenMP C restatement (``gram.c``)."""
+    import ctypes
+    from ._build import load_lib
+    fn = load_lib("gram").oracle_gram_matvec
+    fn.restype = ctypes.c_int
+    fn.argtypes = [ctypes.c_int64, ctypes.c_int64] + [ctypes.c_void_p] * 10
+    X = sp.csr_matrix(X, dtype=np.float64)
+    X.sort_indices()
+    C = sp.csc_matrix(X)
+    C.sort_indices()
+    ip, ix, dv = (np.ascontiguousarray(X.indptr, np.int64), np.ascontiguousarray(X.indices, np.int32),
+                  np.ascontiguousarray(X.data, np.float64))
+    cp, ci, cv = (np.ascontiguousarray(C.indptr, np.int64), np.ascontiguousarray(C.indices, np.int32),
+                  np.ascontiguousarray(C.data, np.float64))
+    Dd = np.ascontiguousarray(D, np.float64)
+    n, m = X.shape
+    t = np.empty(m)
+
+    def f(v):
+        v = np.ascontiguousarray(np.asarray(v, dtype=np.float64).reshape(-1))
+        out = np.empty(n)
+        if fn(n, m, ip.ctypes.data, ix.ctypes.data, dv.ctypes.data, cp.ctypes.data, ci.ctypes.data,
+              cv.ctypes.data, Dd.ctypes.data, v.ctypes.data, t.ctypes.data, out.ctypes.data) != 0:
+            raise ValueError("empty operator")
+        return out
+    return f
+
+
+def eigen(X: sp.csr_matrix, D: np.ndarray, k: int, seed: int, threaded: bool = False):
+    """Same ``eigsh`` call as the reference's embedded ``eigen`` function.
+
+    ``threaded=True`` evaluates the same operator with the OpenMP C matvec
+    (``gram.c``) instead of SciPy's single-threaded CSR products: same
+    ``eigsh`` arguments and start vector, sums equal to FP64 rounding."""
     np.random.seed(seed)
 
     def f(v):
         return X @ (v.T @ X).T - D * v
 
+    if threaded:
+        f = _threaded_matvec(X, D)  # noqa: F811
     n = X.shape[0]
     A = LinearOperator((n, n), matvec=f, dtype=np.float64)
     evals, evecs = eigsh(A, k=k, v0=np.random.rand(n))
@@ -82,14 +119,15 @@ def operator(X: sp.csr_matrix, features=None, feature_weights=None):
 
 
 def spectral(X: sp.csr_matrix, n_vars: int | None = None, features=None, n_comps: int = 30,
-             random_state: int = 0, weighted_by_sd: bool = True, feature_weights=None):
-    """(evals, X_spectral) as ``snap.tl.spectral(..., distance_metric='cosine')`` produces."""
+             random_state: int = 0, weighted_by_sd: bool = True, feature_weights=None, threaded: bool = False):
+    """(evals, X_spectral) as ``snap.tl.spectral(..., distance_metric='cosine')`` produces
+    (``threaded``: the eigensolve's matvec by the OpenMP restatement)."""
     n_obs = X.shape[0]
     n_vars = X.shape[1] if n_vars is None else n_vars
     np.random.seed(random_state)
     n_comps = min(n_vars - 1, n_obs - 1, n_comps)
     Xs, dinv = operator(X, features, feature_weights)
-    evals, evecs = eigen(Xs, dinv, n_comps, random_state)
+    evals, evecs = eigen(Xs, dinv, n_comps, random_state, threaded=threaded)
     if weighted_by_sd:
         idx = [i for i in range(evals.shape[0]) if evals[i] > 0]
         evals = evals[idx]

@@ -526,6 +526,30 @@ def eigsh_lm(op: GramOperator, k: int, *, precision: str = "mixed", block: int =
     return EigenResult(evals, U, info)
 
 
+def residual_norms(op: GramOperator, U: torch.Tensor, evals) -> np.ndarray:
+    """FP64 residuals ||A u_i - λ_i u_i|| of k <= 32 eigenpairs (U: n x k on
+    the device), from one FP64 block matvec: the accuracy check of a result
+    that has no CPU oracle at its size."""
+    L = _lib.load()
+    n, dev = op.n, op.a.device
+    k = int(U.shape[1])
+    kb = 32
+    if k > kb:
+        raise ValueError("residual_norms supports k <= 32")
+    sh = torch.cuda.current_stream(dev).cuda_stream
+    f64 = dict(dtype=torch.float64, device=dev)
+    Up = torch.zeros(n, kb, **f64)
+    Up[:, :k] = U.to(torch.float64)
+    Zs, W = torch.empty(n, kb, **f64), torch.empty(n, kb, **f64)
+    T = torch.empty(op.m, kb, **f64)
+    _lib.check(L.sg_block_finish(1, kb, n, Up.data_ptr(), None, 0, 0, None, Zs.data_ptr(), op.a.data_ptr(), sh),
+               "scale")
+    op.apply(1, kb, Up, Zs, T, W, sh)
+    lam = torch.as_tensor(np.asarray(evals, dtype=np.float64), device=dev)
+    R = W[:, :k] - Up[:, :k] * lam
+    return torch.linalg.vector_norm(R, dim=0).cpu().numpy()
+
+
 def fp64_refine(op: GramOperator, U: torch.Tensor, k: int, stream: int):
     """Final FP64 residual-correction sweep of mixed-precision Ritz pairs.
 
