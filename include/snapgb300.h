@@ -16,7 +16,10 @@
  *    status word `status` (int, set to the first SG_ERR_* seen, 0 otherwise)
  *    and `bad` (uint64, lowest offending input index), which the caller reads
  *    after synchronising.  The reference raises a Rust panic in those cases.
- *  - Entry points are re-entrant per stream; they keep no state.
+ *  - Entry points are re-entrant per stream; they keep no state beyond
+ *    launch-configuration choices made once per process.  sg_lanczos is the
+ *    one call that waits on its stream (once per restart, to read a small
+ *    decision record) and writes host outputs.
  */
 #ifndef SNAPGB300_H
 #define SNAPGB300_H
@@ -420,6 +423,93 @@ int sg_lanczos_hblock(int block, double* H, int64_t ldh, int m0, const double* C
 /* out[:, 0:k] = Q[:, 0:m] Y[0:m, 0:k] (tq/to: 0 = float, 1 = double).       */
 int sg_basis_rotate(int tq, int to, int64_t n, const void* Q, int64_t ldq, int m, const double* Y,
                     int64_t ldy, int k, void* out, int64_t ldo, void* stream);
+
+/* Eigenpairs of a symmetric n x n FP64 matrix on the GPU (n <= 640): the q  */
+/* smallest and p largest eigenvalues (all n when p + q >= n), ascending,    */
+/* into evals (device), their unit eigenvectors as the rows of evecs         */
+/* (device, count x n), largest component positive.  Householder reduction   */
+/* on one thread-block cluster, multisection and inverse iteration.  This is */
+/* the Rayleigh-Ritz step of sg_lanczos, exported for tests and callers.     */
+/* Replaces the small dense eigensolve inside ARPACK (embedding.rs:155-171). */
+int64_t sg_sym_eig_work_bytes(int n, int p, int q);
+int sg_sym_eig(int n, const double* A, int64_t lda, int p, int q, double* evals, double* evecs, void* work,
+               int64_t work_bytes, void* stream);
+
+/* ---- one-call eigensolver: replaces eigen (embedding.rs:155-188) ------- */
+/* The operator A v = a ⊙ (X (w² ⊙ (Xᵀ (a ⊙ v)))) - dinv ⊙ v of one dataset, */
+/* as sg_csr_transpose and sg_spectral_prepare leave it; the reference       */
+/* builds the same operator in spectral_mf (embedding.rs:133-152) and hands  */
+/* it to eigsh.  All pointers are device pointers.                           */
+typedef struct sg_gram_op {
+  int64_t n, m;                                 /* cells, features            */
+  const int64_t* indptr;                        /* X, CSR (n + 1)             */
+  const int32_t* indices;                       /*                            */
+  const float* values;                          /* NULL: binary pattern       */
+  const int64_t* colptr;                        /* X, CSC (m + 1)             */
+  const int32_t* rowidx;                        /*                            */
+  const float* cvalues;                         /* NULL: binary pattern       */
+  const double* w2;                             /* FP64 scalings (m, n, n)    */
+  const double* a;
+  const double* dinv;
+  const float* w2_f32;                          /* FP32 copies (mixed form)   */
+  const float* a_f32;
+  const float* dinv_f32;
+  const void* staged_table_t;                   /* stage-tiled SpMM segment   */
+  const void* staged_table_x;                   /* tables, or NULL            */
+} sg_gram_op;
+
+/* Solver settings; zero / negative fields take the defaults (a NULL opts   */
+/* pointer: all defaults, the correction sweep on, default SpMM kernels).   */
+typedef struct sg_lanczos_opts {
+  int basis;                /* Krylov basis size M (multiple of block)       */
+  int keep;                 /* thick-restart size                            */
+  double tol_vec;           /* residual bar (x max|θ|) of returned vectors   */
+  double tol_val;           /* residual bar of the other wanted pairs        */
+  int vec_positive_only;    /* 1: vectors returned for θ > 0 only (as        */
+                            /* weighted_by_sd keeps), others need tol_val    */
+  int max_restarts;         /* < 0: default 200 (0: no restart)              */
+  int refine;               /* mixed form: final FP64 correction sweep       */
+  int variant_t, variant_x; /* SpMM kernel per pass (codes: < 100 gather,    */
+                            /* 100 + v stage-tiled, 200 + v dynamic); -1:    */
+                            /* library default                               */
+  int refine_variant_t, refine_variant_x; /* FP64 block-32 SpMM of the sweep */
+                            /* (gather or dynamic codes only)                */
+  int time_spmm;            /* 1: CUDA-event time of every SpMM launch       */
+} sg_lanczos_opts;
+
+typedef struct sg_lanczos_info {
+  int64_t block_matvecs;
+  int32_t restarts;
+  int32_t converged;        /* every wanted pair met its bar                 */
+  int32_t basis, keep;
+  double max_residual;      /* largest Ritz residual of the returned pairs   */
+  double next_evals[4];     /* Ritz values just outside the wanted set       */
+  double seconds_cycles;    /* host wall time of the expansion cycles,       */
+  double seconds_ritz;      /* of the GPU Rayleigh-Ritz steps (incl. the     */
+  double seconds_restart;   /* read of their decision), of the restarts and  */
+  double seconds_refine;    /* of the final rotation and correction sweep    */
+  double spmm_ms_t, spmm_ms_x; /* CUDA-event time of the SpMM passes         */
+  int64_t spmm_launches;
+  int64_t kernel_launches;  /* kernels this call launched                    */
+} sg_lanczos_info;
+
+int64_t sg_lanczos_work_bytes(int precision, int block, int k, int64_t n, int64_t m, int basis, int keep);
+
+/* The k eigenpairs of largest magnitude (eigsh which='LM'), eigenvalues     */
+/* descending into evals (host, k), eigenvectors into evecs (device, n x k   */
+/* FP64 row-major), Ritz residual estimates into residuals (host, k; NULL    */
+/* skips).  precision 0: FP32 SpMM and basis, FP64 Rayleigh-Ritz (mixed);    */
+/* 1: all FP64.  block: 4, 8, 16 or 32.  Thick-restart block Lanczos with    */
+/* full reorthogonalisation; the restart's Rayleigh-Ritz runs on the GPU in  */
+/* FP64 (sg_sym_eig) and the host reads one small decision record per        */
+/* restart.  work: caller-owned, 256-byte aligned, sg_lanczos_work_bytes.    */
+/* status: device int (zeroed here).  Returns SG_ERR_NUMERIC for a rank-     */
+/* deficient Krylov block; an unconverged solve is not an error            */
+/* (info->converged = 0).  Host arguments (evals, residuals, info) are       */
+/* written before it returns; evecs is complete when the stream is.         */
+int sg_lanczos(const sg_gram_op* op, int precision, int block, int k, uint64_t seed, const sg_lanczos_opts* opts,
+               void* work, int64_t work_bytes, double* evals, double* evecs, double* residuals,
+               sg_lanczos_info* info, int* status, void* stream);
 
 /* ------------------------------------------------------------------------ */
 /* Exact kNN graph -- replaces nearest_neighbour_graph                       */

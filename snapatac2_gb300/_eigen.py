@@ -14,8 +14,12 @@ reorthogonalisation:
 * block expansion (GPU): W = A Z; two passes of W -= Q (Qᵀ W); two
   Cholesky-QR passes; the Rayleigh-quotient block and the coupling R are
   written into H (FP64) on the device;
-* restart (host, FP64 LAPACK): eigendecomposition of the small H, Ritz
-  residuals ||R y||, convergence test, thick restart Q <- Q Y_keep (GPU).
+* restart (GPU, FP64): eigendecomposition of the small H (cluster
+  Householder reduction, multisection, inverse iteration), Ritz residuals
+  ||R y||, convergence test, thick restart Q <- Q Y_keep.
+
+The whole loop is one C call, ``sg_lanczos`` (``csrc/krylov.cu``); the host
+reads one small decision record per restart.
 
 ``precision='mixed'`` keeps X, the basis and the SpMM in FP32 with FP32
 accumulation (cross-CTA sums in FP64); H, R, the Ritz problem and the output
@@ -23,6 +27,7 @@ vectors are FP64.  ``precision='fp64'`` runs everything in FP64.
 """
 from __future__ import annotations
 
+import ctypes
 import math
 import time
 from dataclasses import dataclass, field
@@ -70,17 +75,8 @@ class GramOperator:
     def apply(self, dtype_code: int, block: int, Z, Zs, T, W, stream: int) -> None:
         """W = A Z (Zs = a ⊙ Z precomputed); T is m x block scratch."""
         vt, vx = self.variants.get((dtype_code, block)) or tune_spmm(self, dtype_code, block, Z, Zs, T, W, stream)
-        ev = SPMM_EVENTS
-        if ev is not None:
-            e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
-            e0.record()
         self.spmm_pass(0, vt, dtype_code, block, Zs, T, stream)
-        if ev is not None:
-            e1.record()
         self.spmm_pass(1, vx, dtype_code, block, T, W, stream, Z)
-        if ev is not None:
-            e2.record()
-            ev.append((e0, e1, e2, self, dtype_code, block))
 
     def spmm_pass(self, which: int, variant: int, dtype_code: int, block: int, inp, out, stream: int,
                   y=None) -> int:
@@ -144,6 +140,10 @@ class GramOperator:
         return t
 
 
+# Largest Ritz problem (basis + block) the GPU Rayleigh-Ritz holds on one
+# thread-block cluster.
+RITZ_MAX = 640
+
 # Residual level (relative to |A|) below which a stalled mixed-precision
 # solve is taken to sit at its FP32 noise floor (~ 2^-24 times a few hundred).
 FP32_FLOOR = 3e-5
@@ -156,7 +156,8 @@ DYN = 200
 _TUNED: dict = {}
 
 
-def tune_spmm(op: "GramOperator", code: int, block: int, Z, Zs, T, W, stream: int) -> tuple[int, int]:
+def tune_spmm(op: "GramOperator", code: int, block: int, Z, Zs, T, W, stream: int,
+              staged: bool = True) -> tuple[int, int]:
     """Pick the fastest SpMM kernel and variant for each pass.
 
     Candidates: the gather kernel's memory-access variants (same arithmetic,
@@ -175,7 +176,7 @@ def tune_spmm(op: "GramOperator", code: int, block: int, Z, Zs, T, W, stream: in
         vt, vx = (int(x) for x in forced.split(","))
         op.variants[(code, block)] = (vt, vx)
         return vt, vx
-    key = (code, block, op.n, op.m, op.csr.nnz >> 20, op.csr.data is not None, op.row_mask is not None)
+    key = (code, block, op.n, op.m, op.csr.nnz >> 20, op.csr.data is not None, op.row_mask is not None, staged)
     if key in _TUNED:
         op.variants[(code, block)] = _TUNED[key]
         return _TUNED[key]
@@ -183,7 +184,7 @@ def tune_spmm(op: "GramOperator", code: int, block: int, Z, Zs, T, W, stream: in
     gather = list(range(int(L.sg_spmm_variants())))
     if code == 1 and block > 8:  # FP64 wide blocks: the deeper unrolls spill
         gather = [v for v in gather if (v & 3) < 2]
-    cands = gather + [STAGED + v for v in range(int(L.sg_spmm_staged_variants()))]
+    cands = gather + ([STAGED + v for v in range(int(L.sg_spmm_staged_variants()))] if staged else [])
     if code == 0:  # FP32: the same gathers on a persistent grid with dynamic row chunks
         cands += [DYN + v for v in gather]
     # private operands: the caller's blocks hold live solver state
@@ -221,8 +222,9 @@ def tune_spmm(op: "GramOperator", code: int, block: int, Z, Zs, T, W, stream: in
     return res
 
 
-# When a list, GramOperator.apply records (start, mid, end) CUDA events around
-# its two SpMM launches, for live per-launch timing by the benchmark.
+# When a list, every eigsh_lm call appends (Xᵀ-pass ms, X-pass ms, block
+# matvecs, operator, precision code, block): sg_lanczos times each of its
+# SpMM launches with CUDA events on its stream, for the benchmark's roofline.
 SPMM_EVENTS: list | None = None
 
 
@@ -366,6 +368,114 @@ def build_operator(csr: DeviceCSR, feature_weights=None, csc=None) -> GramOperat
     return GramOperator(n, m, csr, colptr, rowidx, cval, w, w2, a, dinv, w2_32, a32, dinv32, rinv)
 
 
+# Kernels launched by sg_lanczos calls (the library counts its own launches):
+# the benchmark adds it to its launch tally.
+LANCZOS_LAUNCHES = 0
+
+
+def _spmm_choice(op: GramOperator, code: int, block: int, stream: int, staged: bool = True) -> tuple[int, int]:
+    """Tuned SpMM kernels of (precision, block) for this operator, tuning
+    with scratch blocks of the right shapes on first use.  ``staged=False``
+    (the single block matvec of the correction sweep, whose segment table
+    sg_lanczos is not given) keeps to the gather kernels."""
+    got = op.variants.get((code, block))
+    if got is not None and not staged:
+        got = tuple(v if v < STAGED or v >= DYN else 1 for v in got)
+    if got is None:
+        dev, tdt = op.a.device, _DT["mixed" if code == 0 else "fp64"][1]
+        z = [torch.empty(op.n, block, dtype=tdt, device=dev) for _ in range(3)]
+        t = torch.empty(op.m, block, dtype=tdt, device=dev)
+        got = tune_spmm(op, code, block, z[0], z[1], t, z[2], stream, staged=staged)
+        del z, t
+    for which in (0, 1):  # the stage-tiled kernel needs its segment table
+        if STAGED <= got[which] < DYN:
+            op.staged_table(which, code, block, stream)
+    return got
+
+
+def eigsh_lm(op: GramOperator, k: int, *, precision: str = "mixed", block: int = 8, max_basis: int | None = None,
+             keep: int | None = None, tol_vec: float = 1e-8, tol_val: float = 1e-6, vec_positive_only: bool = True,
+             seed: int = 0, max_restarts: int = 200, stream: torch.cuda.Stream | None = None,
+             refine: bool = True) -> EigenResult:
+    """k eigenpairs of largest magnitude (ARPACK ``which='LM'``) of ``op``,
+    by the library's one-call solver ``sg_lanczos`` (thick-restart block
+    Lanczos; the Rayleigh-Ritz step, the convergence test and the restart run
+    on the GPU in FP64).
+
+    Convergence: every wanted Ritz pair must have ||A y - θ y|| <= tol·max|θ|,
+    with ``tol_vec`` for the pairs whose vectors are returned (the positive
+    ones when ``vec_positive_only``, which ``weighted_by_sd`` keeps) and
+    ``tol_val`` for the rest (whose eigenvalues only decide the LM set).
+    """
+    global LANCZOS_LAUNCHES
+    if precision not in _DT:
+        raise ValueError("precision must be 'mixed' or 'fp64'")
+    if block not in (4, 8, 16, 32):
+        raise ValueError("block must be 4, 8, 16 or 32")
+    L = _lib.lib()
+    code, tdt = _DT[precision]
+    n = op.n
+    dev = op.a.device
+    if k < 1 or k >= n:
+        raise ValueError(f"need 1 <= k < n (k={k}, n={n})")
+    if n <= max(4 * (k + block), 2 * block + 64):
+        return _dense_small(op, k, code, tdt, block)
+    M0, keep0 = _default_basis(k, block, n)
+    M = int(max_basis or M0)
+    keep = int(keep or keep0)
+    M = min(M, (n - block) // block * block)
+    keep = min(keep, M - block)
+    if keep < k or M % block:
+        raise ValueError("basis too small for k")
+    if M + block > RITZ_MAX:
+        raise ValueError(f"basis + block must be at most {RITZ_MAX} (the GPU Rayleigh-Ritz limit)")
+    s = stream or torch.cuda.current_stream(dev)
+    sh = s.cuda_stream
+    t0 = time.perf_counter()
+    vt, vx = _spmm_choice(op, code, block, sh)
+    do_refine = bool(refine and precision == "mixed" and k <= 32)
+    rvt, rvx = _spmm_choice(op, 1, 32, sh, staged=False) if do_refine else (-1, -1)
+    nbytes = int(L.sg_lanczos_work_bytes(code, block, k, n, op.m, M, keep))
+    if nbytes <= 0:
+        raise ValueError("sg_lanczos: unsupported shape")
+    work = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+    tt = op.staged_tables
+    tab_t = tt.get((0, block * (4 if code == 0 else 8)))
+    tab_x = tt.get((1, block * (4 if code == 0 else 8)))
+    csr = op.csr
+    p = lambda t: t.data_ptr() if t is not None else None  # noqa: E731
+    gop = _lib.GramOp(n, op.m, p(csr.indptr), p(csr.indices), p(csr.data), p(op.colptr), p(op.rowidx),
+                      p(op.cvalues), p(op.w2), p(op.a), p(op.dinv), p(op.w2_32), p(op.a32), p(op.dinv32),
+                      p(tab_t), p(tab_x))
+    opts = _lib.LanczosOpts(M, keep, float(tol_vec), float(tol_val), int(bool(vec_positive_only)), int(max_restarts),
+                            int(do_refine), vt, vx, rvt, rvx, int(SPMM_EVENTS is not None))
+    info = _lib.LanczosInfo()
+    evals = np.empty(k, dtype=np.float64)
+    res = np.empty(k, dtype=np.float64)
+    U = torch.empty(n, k, dtype=torch.float64, device=dev)
+    st = _lib.DeviceStatus(dev)
+    rc = L.sg_lanczos(ctypes.byref(gop), code, block, k, int(seed) & 0xFFFFFFFFFFFFFFFF, ctypes.byref(opts),
+                      work.data_ptr(), nbytes, evals.ctypes.data, U.data_ptr(), res.ctypes.data, ctypes.byref(info),
+                      st.status_ptr, sh)
+    if rc == _lib.SG_ERR_NUMERIC:
+        raise _lib.SnapGB300Error(rc, "block Lanczos (rank-deficient Krylov block)")
+    if rc == _lib.SG_ERR_TIMEOUT:
+        raise _lib.SnapGB300Error(rc, "staged SpMM")
+    _lib.check(rc, "sg_lanczos")
+    del work
+    LANCZOS_LAUNCHES += int(info.kernel_launches)
+    if SPMM_EVENTS is not None:
+        SPMM_EVENTS.append((info.spmm_ms_t, info.spmm_ms_x, int(info.spmm_launches) // 2, op, code, block))
+    ph = dict(cycles=info.seconds_cycles, ritz=info.seconds_ritz, restart=info.seconds_restart,
+              refine=info.seconds_refine)
+    out = dict(block_matvecs=int(info.block_matvecs), vector_matvecs=int(info.block_matvecs) * block,
+               restarts=int(info.restarts), basis=int(info.basis), keep=int(info.keep), residuals=res.tolist(),
+               converged=bool(info.converged), seconds=time.perf_counter() - t0, precision=precision, block=block,
+               next_evals=[float(x) for x in info.next_evals if not math.isnan(x)], phase_seconds=ph,
+               kernel_launches=int(info.kernel_launches), spmm_variants=(vt, vx))
+    return EigenResult(evals, U, out)
+
+
 @dataclass
 class EigenResult:
     evals: np.ndarray          # k eigenvalues, descending
@@ -383,11 +493,14 @@ def _default_basis(k: int, block: int, n: int) -> tuple[int, int]:
     return M, keep
 
 
-def eigsh_lm(op: GramOperator, k: int, *, precision: str = "mixed", block: int = 8, max_basis: int | None = None,
-             keep: int | None = None, tol_vec: float = 1e-8, tol_val: float = 1e-6, vec_positive_only: bool = True,
-             seed: int = 0, max_restarts: int = 200, stream: torch.cuda.Stream | None = None,
-             refine: bool = True) -> EigenResult:
-    """k eigenpairs of largest magnitude (ARPACK ``which='LM'``) of ``op``.
+def eigsh_lm_host_ritz(op: GramOperator, k: int, *, precision: str = "mixed", block: int = 8,
+                       max_basis: int | None = None, keep: int | None = None, tol_vec: float = 1e-8,
+                       tol_val: float = 1e-6, vec_positive_only: bool = True, seed: int = 0, max_restarts: int = 200,
+                       stream: torch.cuda.Stream | None = None, refine: bool = True) -> EigenResult:
+    """The same solver driven step by step from Python with the Ritz problem
+    solved on the host (LAPACK): the driver before ``sg_lanczos``, kept to
+    check the one-call solver against it and to time the two Rayleigh-Ritz
+    placements side by side.
 
     Convergence: every wanted Ritz pair must have ||A y - θ y|| <= tol·max|θ|,
     with ``tol_vec`` for the pairs whose vectors are returned (the positive

@@ -107,7 +107,34 @@ SIGNATURES: dict[str, tuple] = {
     "sg_adjoint_final": (_I32, [_I64, _I32, _P, _P, _I32, _P, _P, _P]),
     "sg_square_values": (_I32, [_I64, _P, _P, _P]),
     "sg_basis_rotate": (_I32, [_I32, _I32, _I64, _P, _I64, _I32, _P, _I64, _I32, _P, _I64, _P]),
+    "sg_sym_eig_work_bytes": (_I64, [_I32, _I32, _I32]),
+    "sg_sym_eig": (_I32, [_I32, _P, _I64, _I32, _I32, _P, _P, _P, _I64, _P]),
+    "sg_lanczos_work_bytes": (_I64, [_I32, _I32, _I32, _I64, _I64, _I32, _I32]),
+    "sg_lanczos": (_I32, [_P, _I32, _I32, _I32, ctypes.c_uint64, _P, _P, _I64, _P, _P, _P, _P, _P, _P]),
 }
+
+
+class GramOp(ctypes.Structure):
+    """``sg_gram_op``: the cosine operator of one dataset (device pointers)."""
+    _fields_ = [("n", _I64), ("m", _I64), ("indptr", _P), ("indices", _P), ("values", _P), ("colptr", _P),
+                ("rowidx", _P), ("cvalues", _P), ("w2", _P), ("a", _P), ("dinv", _P), ("w2_f32", _P),
+                ("a_f32", _P), ("dinv_f32", _P), ("staged_table_t", _P), ("staged_table_x", _P)]
+
+
+class LanczosOpts(ctypes.Structure):
+    """``sg_lanczos_opts`` (zero / negative fields take the library defaults)."""
+    _fields_ = [("basis", _I32), ("keep", _I32), ("tol_vec", _F64), ("tol_val", _F64),
+                ("vec_positive_only", _I32), ("max_restarts", _I32), ("refine", _I32), ("variant_t", _I32),
+                ("variant_x", _I32), ("refine_variant_t", _I32), ("refine_variant_x", _I32), ("time_spmm", _I32)]
+
+
+class LanczosInfo(ctypes.Structure):
+    """``sg_lanczos_info``."""
+    _fields_ = [("block_matvecs", _I64), ("restarts", ctypes.c_int32), ("converged", ctypes.c_int32),
+                ("basis", ctypes.c_int32), ("keep", ctypes.c_int32), ("max_residual", _F64),
+                ("next_evals", _F64 * 4), ("seconds_cycles", _F64), ("seconds_ritz", _F64),
+                ("seconds_restart", _F64), ("seconds_refine", _F64), ("spmm_ms_t", _F64), ("spmm_ms_x", _F64),
+                ("spmm_launches", _I64), ("kernel_launches", _I64)]
 
 # Kernels launched by one call of each entry point (launch accounting of the
 # benchmark): e.g. sg_block_cholqr = projection partial + reduce + Cholesky +
@@ -123,6 +150,7 @@ KERNELS_PER_CALL = {
     "sg_square_values": 1,
     "sg_frag_count_lines": 4, "sg_frag_index_lines": 1, "sg_region_plan": 4, "sg_region_run": 5,
     "sg_csr_row_ptr": 4, "sg_csr_copy_rows": 1, "sg_gather_bytes": 1, "sg_nystrom_rescale": 1,
+    "sg_sym_eig": 5,
 }
 
 _lock = threading.Lock()

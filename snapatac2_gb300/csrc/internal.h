@@ -22,6 +22,26 @@ cudaError_t radix_sort_u64(int64_t n, uint64_t* keys, uint64_t* vals, uint64_t* 
                            int begin_bit, int end_bit, void* scratch, cudaStream_t s, bool* in_alt);
 int64_t radix_scratch_bytes(int64_t n);
 
+// Dense symmetric FP64 eigensolver of the Rayleigh-Ritz step (ritz.cu).
+constexpr int kRitzMaxN = 640;  // largest matrix the cluster reduction holds in shared memory
+
+struct RitzLayout {
+  double* d;           // tridiagonal: diagonal
+  double* e;           //              off-diagonal
+  double* tau;         // Householder scalars
+  double* V;           // n x n, row j = reflector j
+  int* ranks;          // ascending ranks of the wanted eigenvalues
+  double* lam;         // their values, ascending
+  double* Zt;          // eigenvectors of the selected ones (rows)
+  double* lu;          // inverse-iteration scratch
+  unsigned char* piv;  //
+  int64_t bytes;
+};
+RitzLayout ritz_layout(char* base, int n, int nw);
+int ritz_values(int n, const double* A, int64_t lda, int p, int q, const RitzLayout& L, int* nw, cudaStream_t s);
+int ritz_vectors(int n, const RitzLayout& L, const int* sel, int nsel, cudaStream_t s);
+int ritz_cluster_size(int n);
+
 inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 
 inline int grid_for(int64_t n, int block, int max_blocks = 1 << 20) {
