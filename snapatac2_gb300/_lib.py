@@ -150,7 +150,7 @@ KERNELS_PER_CALL = {
     "sg_square_values": 1,
     "sg_frag_count_lines": 4, "sg_frag_index_lines": 1, "sg_region_plan": 4, "sg_region_run": 5,
     "sg_csr_row_ptr": 4, "sg_csr_copy_rows": 1, "sg_gather_bytes": 1, "sg_nystrom_rescale": 1,
-    "sg_sym_eig": 5,
+    "sg_sym_eig": 7,
 }
 
 _lock = threading.Lock()

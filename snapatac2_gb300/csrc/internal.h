@@ -35,6 +35,7 @@ struct RitzLayout {
   double* Zt;          // eigenvectors of the selected ones (rows)
   double* lu;          // inverse-iteration scratch
   unsigned char* piv;  //
+  double* G;           // Gram matrix of the selected vectors (Cholesky-QR)
   int64_t bytes;
 };
 RitzLayout ritz_layout(char* base, int n, int nw);

@@ -511,7 +511,7 @@ extern "C" int sg_lanczos(const sg_gram_op* op, int precision, int block, int k,
                                                  tol_vec, tol_val, o.vec_positive_only != 0, status, w.ctl,
                                                  w.theta_keep, w.Yk, w.Bc, w.Yf, w.evals_f, w.res_f);
     SG_CHECK_LAUNCH();
-    nl += 7;
+    nl += 9;
     if (cudaMemcpyAsync(ctl, w.ctl, sizeof(ctl), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
         cudaStreamSynchronize(s) != cudaSuccess)
       return SG_ERR_CUDA;
@@ -567,7 +567,7 @@ extern "C" int sg_lanczos(const sg_gram_op* op, int precision, int block, int k,
     int nw2 = 0;
     SG_TRY(ritz_values(k, w.Cs, k, k, 0, w.ritz32, &nw2, s));
     SG_TRY(ritz_vectors(k, w.ritz32, nullptr, nw2, s));
-    nl += 5;
+    nl += 7;
     refine_finish_kernel<<<1, 256, 0, s>>>(k, w.Ri, w.ritz32.lam, w.ritz32.Zt, w.Yr, w.ev32);
     SG_CHECK_LAUNCH();
     SG_TRY(sg_basis_rotate(1, 1, n, w.Up, kb, k, w.Yr, k, k, evecs, k, s));

@@ -17,7 +17,13 @@
 //              eps·‖T‖ (LAPACK dstebz's default).
 //   invit      eigenvectors of T by inverse iteration with a pivoted
 //              tridiagonal LU (as LAPACK dstein): one warp per cluster of
-//              close eigenvalues, modified Gram-Schmidt inside a cluster.
+//              near-degenerate eigenvalues (1e-9 ‖T‖), modified Gram-Schmidt
+//              inside a cluster.
+//   orth       one FP64 Cholesky-QR of all the vectors (Gram matrix by
+//              warps across the GPU, factor and triangular solve in one CTA):
+//              separately iterated vectors of eigenvalues 1e-9..1e-3 ‖T‖
+//              apart are orthogonal only to eps ‖T‖ / gap; rotating them by
+//              that much moves their residuals by ~eps ‖T‖.
 //   backtr     eigenvectors of A = Q z: one warp per vector applies the
 //              reflectors in reverse order.
 //
@@ -244,7 +250,11 @@ __device__ __forceinline__ double hash_unit(uint64_t a, uint64_t b) {
 // Eigenvectors of T for the selected eigenvalues: sel[0..nsel) are indices
 // into (ranks, lam), ascending (identity when sel is null).  One warp per
 // cluster of selected eigenvalues with consecutive ranks closer than
-// 1e-3 ‖T‖ (LAPACK dstein's rule); inside a cluster the vectors are done in
+// 1e-9 ‖T‖ (near-degenerate pairs).  Outside a cluster a converged vector is
+// within eps ‖T‖ / gap <= 2.2e-7 of its eigenvector, and orth_kernel then
+// restores orthonormality; LAPACK dstein clusters at 1e-3 ‖T‖ instead,
+// which chains the dense bulk of a Ritz spectrum (tiny eigenvalues 1e-7
+// apart) into long sequential runs.  Inside a cluster the vectors are done in
 // order, each orthogonalised against the cluster's earlier ones after every
 // solve (the dot products and updates spread over the lanes).  The pivoted
 // LU and the triangular solves run on lane 0.  lu: per-cluster scratch of 4n
@@ -262,7 +272,7 @@ __global__ void invit_kernel(int n, const double* __restrict__ d, const double* 
     tnorm = fmax(tnorm, fabs(d[i]) + (i > 0 ? fabs(e[i - 1]) : 0.0) + (i + 1 < n ? fabs(e[i]) : 0.0));
 #pragma unroll
   for (int o = 16; o; o >>= 1) tnorm = fmax(tnorm, __shfl_xor_sync(0xffffffffu, tnorm, o));
-  const double ortol = 1e-3 * tnorm;
+  const double ortol = 1e-9 * tnorm;
   auto idx = [&](int w) { return sel ? sel[w] : w; };
   auto joined = [&](int w) {  // selection w continues the cluster of w - 1
     return w > 0 && ranks[idx(w)] == ranks[idx(w - 1)] + 1 && lam[idx(w)] - lam[idx(w - 1)] <= ortol;
@@ -368,6 +378,60 @@ __global__ void invit_kernel(int n, const double* __restrict__ d, const double* 
   }
 }
 
+// G (lower triangle) = Zt Ztᵀ over the nw rows of length n; one warp per entry
+__global__ void gram_rows_kernel(int nw, int n, const double* __restrict__ Zt, double* __restrict__ G) {
+  const int lane = threadIdx.x & 31;
+  const int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t tot = (int64_t)nw * (nw + 1) / 2;
+  if (w >= tot) return;
+  // w -> (i, j), j <= i
+  int i = (int)((sqrt(8.0 * (double)w + 1.0) - 1.0) * 0.5);
+  while ((int64_t)i * (i + 1) / 2 > w) --i;
+  while ((int64_t)(i + 1) * (i + 2) / 2 <= w) ++i;
+  const int j = (int)(w - (int64_t)i * (i + 1) / 2);
+  const double* a = Zt + (size_t)i * n;
+  const double* b = Zt + (size_t)j * n;
+  double s = 0.0;
+  for (int c = lane; c < n; c += 32) s = fma(a[c], b[c], s);
+  s = warp_sum_d(s);
+  if (lane == 0) G[(size_t)i * nw + j] = s;
+}
+
+// Cholesky G = L Lᵀ in place (lower), then Zt <- L⁻¹ Zt (rows orthonormal).
+// One CTA; a non-positive pivot leaves Zt as it is.
+__global__ void __launch_bounds__(1024) orth_kernel(int nw, int n, double* __restrict__ G, double* __restrict__ Zt) {
+  __shared__ int bad;
+  if (threadIdx.x == 0) bad = 0;
+  __syncthreads();
+  for (int j = 0; j < nw; ++j) {
+    if (threadIdx.x == 0) {
+      const double piv = G[(size_t)j * nw + j];
+      if (!(piv > 0.0)) bad = 1;
+      else G[(size_t)j * nw + j] = sqrt(piv);
+    }
+    __syncthreads();
+    if (bad) return;
+    const double ljj = G[(size_t)j * nw + j];
+    for (int i = j + 1 + threadIdx.x; i < nw; i += blockDim.x) G[(size_t)i * nw + j] /= ljj;
+    __syncthreads();
+    // trailing update of the lower triangle: G[i][k] -= L[i][j] L[k][j],
+    // j < k <= i; warp per row, lanes over k
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    for (int i = j + 1 + warp; i < nw; i += nwarps) {
+      const double lij = G[(size_t)i * nw + j];
+      for (int k = j + 1 + lane; k <= i; k += 32) G[(size_t)i * nw + k] -= lij * G[(size_t)k * nw + j];
+    }
+    __syncthreads();
+  }
+  for (int c = threadIdx.x; c < n; c += blockDim.x) {  // forward substitution, one column per thread
+    for (int i = 0; i < nw; ++i) {
+      double y = Zt[(size_t)i * n + c];
+      for (int q = 0; q < i; ++q) y -= G[(size_t)i * nw + q] * Zt[(size_t)q * n + c];
+      Zt[(size_t)i * n + c] = y / G[(size_t)i * nw + i];
+    }
+  }
+}
+
 // Zt rows <- Q Zt rows, Q = H_0 H_1 ... H_{n-3}; one warp per vector
 __global__ void backtr_kernel(int n, const double* __restrict__ V, const double* __restrict__ tau, int nw,
                               double* __restrict__ Zt) {
@@ -469,7 +533,8 @@ RitzLayout ritz_layout(char* base, int n, int nw) {
   auto take = [&](int64_t b) { const int64_t r = o; o += (b + 255) / 256 * 256; return r; };
   const int64_t od = take(8 * (int64_t)n), oe = take(8 * (int64_t)n), ot = take(8 * (int64_t)n),
                 oV = take(8 * (int64_t)n * n), orr = take(4 * (int64_t)n), ol = take(8 * (int64_t)n),
-                oz = take(8 * (int64_t)n * nw), olu = take(32 * (int64_t)n * nw), op = take((int64_t)n * nw);
+                oz = take(8 * (int64_t)n * nw), olu = take(32 * (int64_t)n * nw), op = take((int64_t)n * nw),
+                oG = take(8 * (int64_t)nw * nw);
   if (base) {
     L.d = (double*)(base + od);
     L.e = (double*)(base + oe);
@@ -480,6 +545,7 @@ RitzLayout ritz_layout(char* base, int n, int nw) {
     L.Zt = (double*)(base + oz);
     L.lu = (double*)(base + olu);
     L.piv = (unsigned char*)(base + op);
+    L.G = (double*)(base + oG);
   }
   L.bytes = o;
   return L;
@@ -522,6 +588,13 @@ int ritz_vectors(int n, const RitzLayout& L, const int* sel, int nsel, cudaStrea
     return SG_ERR_CUDA;
   backtr_kernel<<<(nsel + wpb - 1) / wpb, 32 * wpb, sm, s>>>(n, L.V, L.tau, nsel, L.Zt);
   SG_CHECK_LAUNCH();
+  if (nsel > 1) {
+    const int64_t pairs = (int64_t)nsel * (nsel + 1) / 2;
+    gram_rows_kernel<<<grid_for(pairs * 32, 256), 256, 0, s>>>(nsel, n, L.Zt, L.G);
+    SG_CHECK_LAUNCH();
+    orth_kernel<<<1, 1024, 0, s>>>(nsel, n, L.G, L.Zt);
+    SG_CHECK_LAUNCH();
+  }
   return SG_OK;
 }
 
