@@ -51,7 +51,7 @@ def parse():
     p.add_argument("--features", type=int, default=500_000)
     p.add_argument("--nnz", type=float, default=4000.0)
     p.add_argument("--ncomps", type=int, default=30)
-    p.add_argument("--block", type=int, default=8)
+    p.add_argument("--block", type=int, default=0, help="Lanczos block size (0: chosen by the autotuner)")
     p.add_argument("--fp64-steps", type=int, default=3)
     p.add_argument("--oracle-cells", type=int, default=10_000,
                    help="cells of the matrix whose GPU embeddings are compared with the oracle's ARPACK (0: skip)")
@@ -357,18 +357,18 @@ def oracle_accuracy(args, dev, n: int, seed: int):
     Xs, dinv = osp.operator(X)
     ev_o, U_o = osp.eigen(Xs, dinv, args.ncomps, 0, threaded=True)
     out = {"workload": f"{n} cells x {m} features, ~{int(args.nnz)} nnz/cell binary CSR (nnz={csr.nnz}), "
-                       f"n_comps={args.ncomps}, block {args.block}, generator seed {seed}",
+                       f"n_comps={args.ncomps}, block {args.block or 'autotuned'}, generator seed {seed}",
            "oracle": "SciPy ARPACK eigsh(LinearOperator, k, v0=rand(n)) as the reference calls it, FP64, "
                      "matvec by the OpenMP restatement (oracle/gram.c)",
            "oracle_s": time.perf_counter() - t, "oracle_threads": os.cpu_count(),
            "tolerance": "eigenvalues <= 1e-5 relative, principal angles <= 1e-4 rad per cluster of eigenvalues "
                         "within 1e-3 relative"}
     for prec in ("mixed", "fp64"):
-        ev, U, info = spectral_embedding(csr, None, args.ncomps, 0, precision=prec, block=args.block,
+        ev, U, info = spectral_embedding(csr, None, args.ncomps, 0, precision=prec, block=args.block or None,
                                          return_info=True)
         torch.cuda.synchronize(dev)
         nxt = (info.get("next_evals") or [None])[0]
-        out[prec] = {**accuracy_block(ev, U.cpu().numpy(), ev_o, U_o, nxt),
+        out[prec] = {**accuracy_block(ev, U.cpu().numpy(), ev_o, U_o, nxt), "block": info.get("block"),
                      "block_matvecs": info.get("block_matvecs"), "converged": info.get("converged")}
     return out
 
@@ -389,8 +389,9 @@ def large_stage(args, dev):
     csr = DeviceCSR(ip, ix, None, (n, m))
     torch.cuda.synchronize(dev)
     sh = torch.cuda.current_stream(dev).cuda_stream
-    blocks = sorted({args.large_block, args.block}, reverse=True)
     op = _eigen.build_operator(csr)
+    auto = args.block or _eigen.choose_block(op, args.ncomps, "mixed", sh)
+    blocks = sorted({args.large_block, auto}, reverse=True)
     for b in blocks:  # SpMM tuning for this shape class, outside the timed runs
         z = [torch.zeros(n, b, device=dev) for _ in range(3)]
         _eigen.tune_spmm(op, 0, b, z[0], z[1], torch.zeros(m, b, device=dev), z[2], sh)
@@ -419,7 +420,7 @@ def large_stage(args, dev):
                               "knn_s": t3 - t2, "knn_fp64_rescans": int(nfb),
                               "block_matvecs": res.info["block_matvecs"], "restarts": res.info["restarts"],
                               "converged": res.info["converged"]}
-        if keep is None or b == args.block:
+        if keep is None or b == auto:
             keep = (b, op, res, E, nbr, dist)
         del op
     clk = clocks.stop()
@@ -435,12 +436,20 @@ def large_stage(args, dev):
     same, checked = knn_sample_check(E.cpu().numpy(), 50, nbr.cpu().numpy(), dist.cpu().numpy(), 500, seed=12)
     return {"workload": f"{n} cells x {m} features, ~{int(args.nnz)} nnz/cell binary CSR (nnz={csr.nnz}), "
                         f"spectral n_comps={args.ncomps} (mixed) + exact kNN k=50; CSR resident in HBM",
-            "target_wall_s": 30, **runs,
+            "target_wall_s": 30, "autotuned_block": auto,
+            "block_choice_predicted_ms": _block_prediction(op, args.ncomps), **runs,
             "accuracy_vs_fp64_gpu": {**acc, "compared_block": b, "fp64_form_s": t64,
                                      "fp64_block_matvecs": res64.info["block_matvecs"]},
             "max_residual_rel": float(np.max(r) / anorm),
             "residual_note": "FP64 ||A u - λ u|| / max|λ| of the returned mixed-precision eigenpairs",
             "knn_checked_rows": checked, "knn_sample_identical_to_oracle": same, "clocks": clk}
+
+
+def _block_prediction(op, k, precision="mixed"):
+    """The block autotuner's predicted seconds per candidate for this shape."""
+    from snapatac2_gb300 import _eigen
+    got = _eigen._BLOCK_CHOICE.get(_eigen._shape_class(op, _eigen._DT[precision][0], k))
+    return {str(b): round(v, 3) for b, v in got[1].items()} if got else None
 
 
 def knn_sample_check(X: np.ndarray, k: int, nbr: np.ndarray, dist: np.ndarray, n_rows: int, seed: int,
@@ -490,7 +499,7 @@ def e2e_breakdown(snap, ad, args, dev):
     try:
         torch.cuda.synchronize(dev)
         t = time.perf_counter()
-        snap.tl.spectral(ad, features=None, n_comps=args.ncomps, block=args.block)
+        snap.tl.spectral(ad, features=None, n_comps=args.ncomps, block=args.block or None)
         torch.cuda.synchronize(dev)
         total = time.perf_counter() - t
     finally:
@@ -556,7 +565,7 @@ def run_gpu(args):
     nnz = csr.nnz
 
     def step(precision="mixed"):
-        return spectral_embedding(csr, None, args.ncomps, 0, precision=precision, block=args.block,
+        return spectral_embedding(csr, None, args.ncomps, 0, precision=precision, block=args.block or None,
                                   return_info=True)
 
     def barrier():
@@ -623,7 +632,7 @@ def run_gpu(args):
         ad = snap.AnnData(n_obs=n, n_vars=m)
         ad.X = host
         h2d = host.indptr.numel() * 8 + host.indices.numel() * 4
-        snap.tl.spectral(ad, features=None, n_comps=args.ncomps, block=args.block)  # warm
+        snap.tl.spectral(ad, features=None, n_comps=args.ncomps, block=args.block or None)  # warm
 
         def raw_h2d():  # the copy alone, pinned host -> device, three times
             out = []
@@ -641,7 +650,7 @@ def run_gpu(args):
         t0 = time.perf_counter()
         step_ends = []
         for _ in range(args.e2e_steps):
-            snap.tl.spectral(ad, features=None, n_comps=args.ncomps, block=args.block)
+            snap.tl.spectral(ad, features=None, n_comps=args.ncomps, block=args.block or None)
             step_ends.append(time.perf_counter())  # the call returns host arrays: already synchronised
         torch.cuda.synchronize(dev)
         e2e_ms = (time.perf_counter() - t0) * 1e3 / args.e2e_steps
@@ -689,7 +698,7 @@ def run_gpu(args):
                                                                  / np.sort(np.abs(ev64))))}
 
     # ---- gather floor of the SpMM passes (diagnostic, after the timed legs) --
-    gather = gather_ceiling(csr, args.block, dev) if rank == 0 else None
+    gather = gather_ceiling(csr, infos[-1]["block"], dev) if rank == 0 else None
     if gather is not None:
         nl = max(n_apply, 1)
         gather.update({"xt_spmm_ms": t_time / nl, "x_spmm_ms": x_time / nl,
@@ -725,7 +734,8 @@ def run_gpu(args):
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": f"spectral embedding, {n} cells x {m} features, ~{int(args.nnz)} nnz/cell binary CSR "
                                f"(nnz={nnz}), n_comps={args.ncomps}, mixed precision",
-                   "parallelism": "replicas" if world > 1 else "single GPU", "block": args.block,
+                   "parallelism": "replicas" if world > 1 else "single GPU", "block": info["block"],
+                   "block_choice": "given" if args.block else "autotuned (choose_block)",
                    "l2": "inputs larger than L2 (CSR indices 4 B x nnz)",
                    "block_matvecs": info["block_matvecs"], "restarts": info["restarts"], "basis": info["basis"],
                    "phase_seconds": info.get("phase_seconds")},
@@ -793,13 +803,13 @@ def run_batched(args):
 
     def batched():
         bop = _batched.build_batched_operator(mats)
-        return _batched.eigsh_lm_batched(bop, args.ncomps, block=args.block)
+        return _batched.eigsh_lm_batched(bop, args.ncomps, block=args.block or 8)
 
     def one_by_one():
         out = []
         for c in mats:
             op = _eigen.build_operator(c)
-            out.append(_eigen.eigsh_lm(op, args.ncomps, block=args.block))
+            out.append(_eigen.eigsh_lm(op, args.ncomps, block=args.block or 8))
         return out
 
     for _ in range(max(1, args.warmup - 2)):
@@ -835,7 +845,7 @@ def run_batched(args):
             "unit": "cells/s", "n_gpus": 1, "steps": 1, "warmup": max(1, args.warmup - 2), "ms_per_step": tb * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": f"{D} datasets, {n_tot} cells total ({ns.min()}-{ns.max()}), features "
-                                   f"{ms.min()}-{ms.max()}, 2-20 clusters, nnz {nnz}", "block": args.block},
+                                   f"{ms.min()}-{ms.max()}, 2-20 clusters, nnz {nnz}", "block": args.block or 8},
             "batched": res.info, "one_by_one_s": ts, "one_by_one_cells_per_s": n_tot / ts,
             "max_eval_rel_diff_batched_vs_single": err, "knn15_all_datasets_s": tk}
     print(json.dumps(line), flush=True)

@@ -393,7 +393,8 @@ def _spmm_choice(op: GramOperator, code: int, block: int, stream: int, staged: b
     return got
 
 
-def eigsh_lm(op: GramOperator, k: int, *, precision: str = "mixed", block: int = 8, max_basis: int | None = None,
+def eigsh_lm(op: GramOperator, k: int, *, precision: str = "mixed", block: int | None = 8,
+             max_basis: int | None = None,
              keep: int | None = None, tol_vec: float = 1e-8, tol_val: float = 1e-6, vec_positive_only: bool = True,
              seed: int = 0, max_restarts: int = 200, stream: torch.cuda.Stream | None = None,
              refine: bool = True) -> EigenResult:
@@ -406,18 +407,22 @@ def eigsh_lm(op: GramOperator, k: int, *, precision: str = "mixed", block: int =
     with ``tol_vec`` for the pairs whose vectors are returned (the positive
     ones when ``vec_positive_only``, which ``weighted_by_sd`` keeps) and
     ``tol_val`` for the rest (whose eigenvalues only decide the LM set).
+    ``block=None`` lets ``choose_block`` pick the block size.
     """
     global LANCZOS_LAUNCHES
     if precision not in _DT:
         raise ValueError("precision must be 'mixed' or 'fp64'")
-    if block not in (4, 8, 16, 32):
-        raise ValueError("block must be 4, 8, 16 or 32")
     L = _lib.lib()
     code, tdt = _DT[precision]
     n = op.n
     dev = op.a.device
     if k < 1 or k >= n:
         raise ValueError(f"need 1 <= k < n (k={k}, n={n})")
+    chosen = block is None
+    if chosen:
+        block = choose_block(op, k, precision, stream.cuda_stream if stream is not None else None)
+    if block not in (4, 8, 16, 32):
+        raise ValueError("block must be 4, 8, 16 or 32")
     if n <= max(4 * (k + block), 2 * block + 64):
         return _dense_small(op, k, code, tdt, block)
     M0, keep0 = _default_basis(k, block, n)
@@ -464,6 +469,8 @@ def eigsh_lm(op: GramOperator, k: int, *, precision: str = "mixed", block: int =
     _lib.check(rc, "sg_lanczos")
     del work
     LANCZOS_LAUNCHES += int(info.kernel_launches)
+    if max_basis is None and info.converged:  # convergence history of the block choice
+        _BLOCK_SEEN.setdefault(_shape_class(op, code, k), {})[block] = int(info.block_matvecs) * block
     if SPMM_EVENTS is not None:
         SPMM_EVENTS.append((info.spmm_ms_t, info.spmm_ms_x, int(info.spmm_launches) // 2, op, code, block))
     ph = dict(cycles=info.seconds_cycles, ritz=info.seconds_ritz, restart=info.seconds_restart,
@@ -472,7 +479,7 @@ def eigsh_lm(op: GramOperator, k: int, *, precision: str = "mixed", block: int =
                restarts=int(info.restarts), basis=int(info.basis), keep=int(info.keep), residuals=res.tolist(),
                converged=bool(info.converged), seconds=time.perf_counter() - t0, precision=precision, block=block,
                next_evals=[float(x) for x in info.next_evals if not math.isnan(x)], phase_seconds=ph,
-               kernel_launches=int(info.kernel_launches), spmm_variants=(vt, vx))
+               kernel_launches=int(info.kernel_launches), spmm_variants=(vt, vx), block_chosen=chosen)
     return EigenResult(evals, U, out)
 
 
@@ -491,6 +498,128 @@ def _default_basis(k: int, block: int, n: int) -> tuple[int, int]:
     M = keep + max(15 * block, 96)
     M = int(math.ceil(M / block) * block)
     return M, keep
+
+
+# Vector matvecs a solve needs at each block size, relative to block 8 (k =
+# 30, tol 1e-8): 100,000 cells 0.68 / 1 / 1.32 / 1.96 and 1,000,000 cells
+# - / 1 / 1.46 / 2.40 for blocks 4 / 8 / 16 / 32.  The prior of the block
+# choice; observed solves of the same shape class replace it.
+BLOCK_PRIOR = {4: 0.68, 8: 1.0, 16: 1.39, 32: 2.18}
+_BLOCK_CHOICE: dict = {}   # shape class -> (block, predicted seconds per block)
+_BLOCK_SEEN: dict = {}     # shape class -> {block: vector matvecs of the last solve}
+_RITZ_MS: dict = {}        # basis size -> measured ms of one GPU Rayleigh-Ritz step
+
+
+def _shape_class(op: GramOperator, code: int, k: int):
+    return (code, op.n, op.m, op.csr.nnz >> 20, op.csr.data is not None, k)
+
+
+def _ritz_ms(M: int, keep: int, stream: int) -> float:
+    """Measured time of one GPU Rayleigh-Ritz step at basis M (cached)."""
+    if M in _RITZ_MS:
+        return _RITZ_MS[M]
+    L = _lib.load()
+    dev = torch.device("cuda", torch.cuda.current_device())
+    g = torch.Generator(device="cpu").manual_seed(M)
+    A = torch.randn(M, M, generator=g, dtype=torch.float64)
+    A = (0.5 * (A + A.T)).to(dev)
+    p = min(M, keep + 4)
+    nb = int(L.sg_sym_eig_work_bytes(M, p, p))
+    work = torch.empty(nb, dtype=torch.uint8, device=dev)
+    nw = M if 2 * p >= M else 2 * p
+    ev = torch.empty(nw, dtype=torch.float64, device=dev)
+    vec = torch.empty(nw, M, dtype=torch.float64, device=dev)
+    run = lambda: _lib.check(L.sg_sym_eig(M, A.data_ptr(), M, p, p, ev.data_ptr(), vec.data_ptr(),  # noqa: E731
+                                          work.data_ptr(), nb, stream), "sg_sym_eig")
+    run()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    run()
+    e1.record()
+    e1.synchronize()
+    _RITZ_MS[M] = e0.elapsed_time(e1)
+    return _RITZ_MS[M]
+
+
+def _block_step_ms(op: GramOperator, code: int, b: int, ncols: int, ld: int, stream: int) -> float:
+    """CUDA-event time of one block step at block b: the operator with the
+    default SpMM kernels, two Gram-Schmidt passes against ncols basis
+    vectors, two Cholesky-QR passes (scratch operands)."""
+    L = _lib.load()
+    dev = op.a.device
+    tdt = torch.float32 if code == 0 else torch.float64
+    n = op.n
+    Q = torch.empty(n, ld, dtype=tdt, device=dev)
+    Z, Zs, W = (torch.empty(n, b, dtype=tdt, device=dev) for _ in range(3))
+    T = torch.empty(op.m, b, dtype=tdt, device=dev)
+    nparts = int(L.sg_proj_parts())
+    f64 = dict(dtype=torch.float64, device=dev)
+    part, C = torch.empty(nparts * ld * b, **f64), torch.empty(ld * b, **f64)
+    G, R, Ri = (torch.empty(b * b, **f64) for _ in range(3))
+    st = _lib.DeviceStatus(dev)
+    for t in (Q, Z, Zs, W):
+        _lib.check(L.sg_fill_random(code, t.numel(), 7, t.data_ptr(), stream), "fill")
+    vt, vx = (DYN + 7, 6) if code == 0 else (1, 1)
+
+    def step():
+        op.spmm_pass(0, vt, code, b, Zs, T, stream)
+        op.spmm_pass(1, vx, code, b, T, W, stream, Z)
+        for _ in range(2):
+            L.sg_block_proj(code, b, n, Q.data_ptr(), ld, ncols, W.data_ptr(), part.data_ptr(), nparts,
+                            C.data_ptr(), stream)
+            L.sg_block_update(code, b, n, Q.data_ptr(), ld, ncols, C.data_ptr(), W.data_ptr(), stream)
+        for _ in range(2):
+            L.sg_block_cholqr(code, b, n, W.data_ptr(), part.data_ptr(), nparts, G.data_ptr(), R.data_ptr(),
+                              Ri.data_ptr(), st.status_ptr, stream)
+    step()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    step()
+    e1.record()
+    e1.synchronize()
+    return e0.elapsed_time(e1)
+
+
+def choose_block(op: GramOperator, k: int, precision: str = "mixed", stream: int | None = None,
+                 candidates=(4, 8, 16, 32)) -> int:
+    """Lanczos block size for this operator, chosen once per shape class
+    (precision, n, m, nnz, valued, k) and process.
+
+    For each candidate b the predicted solve time is
+      V(b)/b x (one block step, measured) + V(b)/(M_b - keep_b) x (one GPU
+      Rayleigh-Ritz step at basis M_b, measured),
+    with V(b) the vector matvecs the solve needs: the observed count of an
+    earlier solve of this shape class at block b, else BLOCK_PRIOR scaled by
+    the observed counts at other blocks.  Block steps are timed on scratch
+    operands with the default SpMM kernels (the kernels are tuned afterwards
+    for the chosen block only: tuning every block costs seconds at 1M cells).
+    """
+    code = _DT[precision][0]
+    key = _shape_class(op, code, k)
+    if key in _BLOCK_CHOICE:
+        return _BLOCK_CHOICE[key][0]
+    n = op.n
+    dev = op.a.device
+    sh = stream if stream is not None else torch.cuda.current_stream(dev).cuda_stream
+    seen = _BLOCK_SEEN.get(key, {})
+    scale = np.mean([v / BLOCK_PRIOR[b] for b, v in seen.items()]) if seen else 1.0
+    best, pred = 8, {}
+    for b in candidates:
+        if n <= max(4 * (k + b), 2 * b + 64):
+            continue
+        M, keep = _default_basis(k, b, n)
+        M = min(M, (n - b) // b * b)
+        keep = min(keep, M - b)
+        if keep < k or M + b > RITZ_MAX:
+            continue
+        V = seen.get(b, BLOCK_PRIOR[b] * scale)
+        t_step = _block_step_ms(op, code, b, (keep + M) // 2, M + b, sh)
+        t_rr = _ritz_ms(M, keep, sh)
+        pred[b] = V / b * t_step + V / (M - keep) * t_rr
+    if pred:
+        best = min(pred, key=pred.get)
+    _BLOCK_CHOICE[key] = (best, pred)
+    return best
 
 
 def eigsh_lm_host_ritz(op: GramOperator, k: int, *, precision: str = "mixed", block: int = 8,

@@ -125,7 +125,7 @@ def release_uploads(borrowed: list) -> None:
 
 
 def spectral_embedding(X, features=None, n_comps: int = 30, random_state: int = 0, feature_weights=None, *,
-                       precision: str = "mixed", block: int = 8, device=None, return_info: bool = False,
+                       precision: str = "mixed", block: int | None = None, device=None, return_info: bool = False,
                        **solver_kw):
     """(evals, evecs) of the normalised cosine operator, like the PyO3
     ``spectral_embedding`` (``snapatac2-python/src/embedding.rs:24-59``):
@@ -166,7 +166,7 @@ def spectral(
     inplace: bool = True,
     *,
     precision: Literal["auto", "mixed", "fp64"] = "auto",
-    block: int = 8,
+    block: int | None = None,
     device=None,
 ):
     """Laplacian-eigenmap embedding (``_embedding.py:129-295``), cosine; the full
@@ -177,7 +177,7 @@ def spectral(
     'auto' (default): FP64 below ``AUTO_FP64_CELLS`` cells, where it is cheap
     and where the top eigenvalues reach into a dense bulk whose gaps are
     comparable to the FP32 noise floor, mixed above), ``block`` (Lanczos
-    block size), ``device``.
+    block size; None: chosen by the autotuner per shape class), ``device``.
     """
     np.random.seed(random_state)
     if isinstance(features, str):

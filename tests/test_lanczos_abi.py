@@ -210,3 +210,20 @@ def test_sg_lanczos_refuses_bad_arguments():
     assert call(8, 0, nb) == _lib.SG_ERR_ARG         # k < 1
     assert call(8, 10, nb - 256) == _lib.SG_ERR_CAP  # workspace too small
     assert int(L.sg_lanczos_work_bytes(0, 32, 30, 10**6, 5 * 10**5, 640, 0)) == -1  # Ritz problem above 640
+
+
+@pytest.mark.gpu
+def test_block_autotuner_choice_is_cached_and_solves_to_the_oracle():
+    from snapatac2_gb300 import _eigen
+    X, op = _operator(n=5000, m=60000, nnz=500, seed=33)
+    b = _eigen.choose_block(op, 30, "mixed")
+    assert b in (4, 8, 16, 32)
+    key = _eigen._shape_class(op, 0, 30)
+    best, pred = _eigen._BLOCK_CHOICE[key]
+    assert best == b and b in pred and all(v > 0 for v in pred.values())
+    assert _eigen.choose_block(op, 30, "mixed") == b  # cached per shape class
+    r = _eigen.eigsh_lm(op, 30, block=None)
+    assert r.info["block"] == b and r.info["block_chosen"] and r.info["converged"]
+    assert _eigen._BLOCK_SEEN[key][b] == r.info["vector_matvecs"]  # convergence history recorded
+    ev_ref, U_ref = osp.eigen(*osp.operator(X), 30, 0)
+    check_eigs(r.evals, r.evecs.cpu().numpy(), ev_ref, U_ref)
