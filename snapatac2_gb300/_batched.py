@@ -390,3 +390,49 @@ def spectral_batched(mats, n_comps: int = 30, *, precision: str = "auto", block:
             E = E[:, idx] * np.sqrt(ev)
         out.append((ev, E))
     return out
+
+
+def embed_concurrent(mats, n_comps: int = 30, *, precision: str = "mixed", block: int | None = 8,
+                     streams: int = 8, **kw) -> list:
+    """Embed independent datasets concurrently: each dataset is one
+    build_operator + sg_lanczos solve on its own CUDA stream, from a pool of
+    ``streams`` host threads (sg_lanczos runs its whole restart loop in the
+    library with the GIL released, so the threads' launches and their
+    per-restart decisions overlap).  Datasets start largest first; each
+    leaves as soon as its own solve has converged, so small datasets never
+    wait for large ones and the GPU keeps several solves in flight.
+
+    Returns the list of EigenResult, in the order of ``mats``; each equals a
+    separate eigsh_lm of that dataset (same kernels, same arithmetic).
+    """
+    dev = torch.device("cuda", torch.cuda.current_device())
+    order = sorted(range(len(mats)), key=lambda d: -int(mats[d].nnz))
+    pool_streams = [torch.cuda.Stream(device=dev) for _ in range(max(1, streams))]
+    free = list(range(len(pool_streams)))
+    import threading
+    lock = threading.Lock()
+    out: list = [None] * len(mats)
+    # the caller's work on its current stream precedes every solve
+    start = torch.cuda.Event()
+    start.record(torch.cuda.current_stream(dev))
+
+    def run(d):
+        with lock:
+            si = free.pop()
+        s = pool_streams[si]
+        try:
+            torch.cuda.set_device(dev)
+            s.wait_event(start)
+            with torch.cuda.stream(s):
+                op = _eigen.build_operator(mats[d])
+                out[d] = _eigen.eigsh_lm(op, n_comps, precision=precision, block=block, stream=s, **kw)
+                del op
+            s.synchronize()
+        finally:
+            with lock:
+                free.append(si)
+
+    with ThreadPoolExecutor(max_workers=len(pool_streams)) as ex:
+        for f in [ex.submit(run, d) for d in order]:
+            f.result()
+    return out

@@ -29,6 +29,7 @@ from __future__ import annotations
 
 import ctypes
 import math
+import threading
 import time
 from dataclasses import dataclass, field
 
@@ -371,6 +372,7 @@ def build_operator(csr: DeviceCSR, feature_weights=None, csc=None) -> GramOperat
 # Kernels launched by sg_lanczos calls (the library counts its own launches):
 # the benchmark adds it to its launch tally.
 LANCZOS_LAUNCHES = 0
+_COUNT_LOCK = threading.Lock()
 
 
 def _spmm_choice(op: GramOperator, code: int, block: int, stream: int, staged: bool = True) -> tuple[int, int]:
@@ -468,7 +470,8 @@ def eigsh_lm(op: GramOperator, k: int, *, precision: str = "mixed", block: int |
         raise _lib.SnapGB300Error(rc, "staged SpMM")
     _lib.check(rc, "sg_lanczos")
     del work
-    LANCZOS_LAUNCHES += int(info.kernel_launches)
+    with _COUNT_LOCK:
+        LANCZOS_LAUNCHES += int(info.kernel_launches)
     if max_basis is None and info.converged:  # convergence history of the block choice
         _BLOCK_SEEN.setdefault(_shape_class(op, code, k), {})[block] = int(info.block_matvecs) * block
     if SPMM_EVENTS is not None:

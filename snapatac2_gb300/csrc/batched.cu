@@ -453,7 +453,7 @@ extern "C" int sg_bbasis_rotate(int tq, int to, int ncta, const int* cta_ds, con
   do {                                                                                                       \
     if (smem > 48 * 1024 &&                                                                                  \
         cudaFuncSetAttribute(brotate_kernel<TQ, TA, TO>, cudaFuncAttributeMaxDynamicSharedMemorySize,        \
-                             (int)smem) != cudaSuccess)                                                      \
+                             200 * 1024) != cudaSuccess)                                                     \
       return SG_ERR_CUDA;                                                                                    \
     brotate_kernel<TQ, TA, TO><<<grid, 256, smem, s>>>(cta_ds, cta_r0, cta_r1, (const TQ*)Q, ldq, m, Y, ldy, \
                                                        ystride, k, (TO*)out, ldo);                           \

@@ -431,11 +431,15 @@ int update_dispatch(int B, int64_t n, const T* Q, int64_t ldq, int ncols, const 
   const int grid = grid_for(n * 32, 256, 8 * sm_count_l());
   const size_t smem = (size_t)ncols * B * sizeof(T);
   if (smem > 200 * 1024) return SG_ERR_ARG;
+  // dynamic shared memory caps are set to the largest size (200 KB) any call
+  // needs, never to one call's size: host threads embedding datasets of
+  // different sizes concurrently would otherwise lower the cap between
+  // another thread's set and its launch
 #define SG_UPD(BB)                                                                                   \
   case BB:                                                                                           \
     if (smem > 48 * 1024 &&                                                                          \
         cudaFuncSetAttribute(update_kernel<T, BB>, cudaFuncAttributeMaxDynamicSharedMemorySize,      \
-                             (int)smem) != cudaSuccess)                                              \
+                             200 * 1024) != cudaSuccess)                                             \
       return SG_ERR_CUDA;                                                                            \
     update_kernel<T, BB><<<grid, 256, smem, s>>>(n, Q, ldq, ncols, C, W);                            \
     break;
@@ -566,7 +570,7 @@ extern "C" int sg_basis_rotate(int tq, int to, int64_t n, const void* Q, int64_t
   do {                                                                                                  \
     if (smem > 48 * 1024 &&                                                                             \
         cudaFuncSetAttribute(rotate_kernel<TQ, TA, TO>, cudaFuncAttributeMaxDynamicSharedMemorySize,    \
-                             (int)smem) != cudaSuccess)                                                 \
+                             200 * 1024) != cudaSuccess)                                                \
       return SG_ERR_CUDA;                                                                               \
     rotate_kernel<TQ, TA, TO><<<grid, 256, smem, s>>>(n, (const TQ*)Q, ldq, m, Y, ldy, k, (TO*)out, ldo); \
   } while (0)

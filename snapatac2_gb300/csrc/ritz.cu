@@ -472,7 +472,10 @@ int launch_tridiag_cs(int n, const double* A, int64_t lda, double* d, double* e,
                       cudaStream_t s, bool probe_only) {
   const size_t smem = tridiag_smem(n, CS);
   if (smem > 227 * 1024) return SG_ERR_ARG;
-  if (cudaFuncSetAttribute(tridiag_kernel<CS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+  // the cap is set to the largest size any call needs, never to this call's:
+  // calls on other host threads set the same value, so none can lower the
+  // cap between another thread's set and its launch
+  if (cudaFuncSetAttribute(tridiag_kernel<CS>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024) !=
       cudaSuccess)
     return SG_ERR_CUDA;
   if (CS > 8 && cudaFuncSetAttribute(tridiag_kernel<CS>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
@@ -581,11 +584,9 @@ int ritz_vectors(int n, const RitzLayout& L, const int* sel, int nsel, cudaStrea
   invit_kernel<<<grid_for((int64_t)nsel * 32, 128), 128, 0, s>>>(n, L.d, L.e, L.ranks, L.lam, sel, nsel, L.Zt, L.lu,
                                                                   L.piv);
   SG_CHECK_LAUNCH();
-  const int wpb = 4;
+  constexpr int wpb = 4;
   const size_t sm = (size_t)wpb * n * sizeof(double);
-  if (sm > 48 * 1024 &&
-      cudaFuncSetAttribute(backtr_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess)
-    return SG_ERR_CUDA;
+  static_assert(wpb * kRitzMaxN * sizeof(double) <= 48 * 1024, "back-transformation fits default shared memory");
   backtr_kernel<<<(nsel + wpb - 1) / wpb, 32 * wpb, sm, s>>>(n, L.V, L.tau, nsel, L.Zt);
   SG_CHECK_LAUNCH();
   if (nsel > 1) {

@@ -50,3 +50,24 @@ def test_batched_weighted_output_matches_single():
         e2, E2 = osp.spectral(X, n_comps=20)
         assert ev.shape == e2.shape and np.allclose(ev, e2, rtol=1e-5)
         assert E.shape == E2.shape
+
+
+@pytest.mark.gpu
+def test_concurrent_embedding_matches_separate_solves():
+    """embed_concurrent (one sg_lanczos per dataset on a pool of streams)
+    gives each dataset the eigenpairs of a separate solve."""
+    import torch
+    from snapatac2_gb300 import _batched, _eigen
+    from snapatac2_gb300._binning import DeviceCSR
+    from test_spectral import check_eigs
+    dev = torch.device("cuda")
+    mats = []
+    for d, (n, m) in enumerate([(6000, 40000), (2500, 30000), (9000, 50000), (3000, 20000), (4500, 45000)]):
+        B = syn.binary_csr(n, m, nnz_per_cell=300, n_clusters=3 + d, enriched=m // 10, seed=50 + d)
+        mats.append(DeviceCSR(torch.from_numpy(B.indptr).to(dev), torch.from_numpy(B.indices).to(dev), None,
+                              B.shape))
+    conc = _batched.embed_concurrent(mats, 20, block=8, streams=3)
+    for c, r in zip(mats, conc):
+        ref = _eigen.eigsh_lm(_eigen.build_operator(c), 20, block=8)
+        assert r.info["converged"]
+        check_eigs(r.evals, r.evecs.cpu().numpy(), ref.evals, ref.evecs.cpu().numpy(), rtol=1e-9, angle=1e-6)
