@@ -582,6 +582,13 @@ int sg_adjoint_final(int64_t m, int k, const double* w, const double* zeh, int b
 /* out[t] = values[t]^2 (the X∘X values of the third SpMM). */
 int sg_square_values(int64_t nnz, const float* values, float* out, void* stream);
 
+/* Test hook (no counterpart in the reference): the stage-tiled SpMM skips  */
+/* the copies of stage skip_stage, so that stage's bounded wait runs out    */
+/* with nothing in flight (status SG_ERR_TIMEOUT, the kernel returns), and  */
+/* every stage wait gives up after wait_ns.  skip_stage < 0, wait_ns <= 0:  */
+/* normal operation.  Synchronous; process-wide; for failure tests only.    */
+int sg_test_staged_fault(int skip_stage, int64_t wait_ns);
+
 /* Allocation-free sg_knn (no counterpart in the reference).  Same inputs,   */
 /* outputs and result as sg_knn, for callers that cannot allocate device    */
 /* memory: the scratch is a fixed array inside the library (about 33 MB per  */

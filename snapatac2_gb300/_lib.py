@@ -107,6 +107,7 @@ SIGNATURES: dict[str, tuple] = {
     "sg_adjoint_final": (_I32, [_I64, _I32, _P, _P, _I32, _P, _P, _P]),
     "sg_square_values": (_I32, [_I64, _P, _P, _P]),
     "sg_basis_rotate": (_I32, [_I32, _I32, _I64, _P, _I64, _I32, _P, _I64, _I32, _P, _I64, _P]),
+    "sg_test_staged_fault": (_I32, [_I32, _I64]),
     "sg_sym_eig_work_bytes": (_I64, [_I32, _I32, _I32]),
     "sg_sym_eig": (_I32, [_I32, _P, _I64, _I32, _I32, _P, _P, _P, _I64, _P]),
     "sg_lanczos_work_bytes": (_I64, [_I32, _I32, _I32, _I64, _I64, _I32, _I32]),

@@ -174,8 +174,9 @@ __device__ __forceinline__ uint64_t global_ns() {
 }
 
 // Wait for the phase with this parity to complete; gives up (false) after
-// kWaitNs of wall time, so a copy that never lands cannot hang the kernel.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+// limit_ns of wall time (kWaitNs by default), so a copy that never lands
+// cannot hang the kernel.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint64_t limit_ns = kWaitNs) {
   const uint64_t t0 = global_ns();
   while (true) {
     uint32_t done;
@@ -185,7 +186,7 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
         : "r"(smem_u32(bar)), "r"(parity)
         : "memory");
     if (done) return true;
-    if (global_ns() - t0 > kWaitNs) return false;
+    if (global_ns() - t0 > limit_ns) return false;
   }
 }
 

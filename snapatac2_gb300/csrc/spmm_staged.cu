@@ -125,6 +125,13 @@ __global__ void staged_table_kernel(int64_t rows, int64_t cols, const int64_t* _
   }
 }
 
+// Failure injection for tests (set only by sg_test_staged_fault): the stage
+// whose copies thread 0 does not issue, so its barrier never completes and
+// nothing is in flight for it, and the limit of every stage wait.  -1 and
+// kWaitNs in normal operation.
+__device__ int g_staged_skip_stage = -1;
+__device__ unsigned long long g_staged_wait_ns = kWaitNs;
+
 template <typename T, int B, bool VALUED, int SGL, int U>
 __global__ void __launch_bounds__(kStagedThreads, 1)
 spmm_staged_kernel(int64_t rows, int64_t cols, int64_t rows_per_cta, int64_t rpc4, int64_t stage_cols,
@@ -154,7 +161,10 @@ spmm_staged_kernel(int64_t rows, int64_t cols, int64_t rows_per_cta, int64_t rpc
   const int32_t* ridx = idx + base;
   const float* rval = VALUED ? val + base : nullptr;
 
+  const int64_t skip_stage = g_staged_skip_stage;
+  const uint64_t wait_ns = g_staged_wait_ns;
   auto issue = [&](int64_t k) {
+    if (k == skip_stage) return;  // test hook: this stage's barrier never completes
     const int64_t lo = k * stage_cols;
     const int64_t cnt = min(stage_cols, cols - lo);
     uint64_t* b = &bar[k & 1];
@@ -184,12 +194,12 @@ spmm_staged_kernel(int64_t rows, int64_t cols, int64_t rows_per_cta, int64_t rpc
   constexpr int kGroups = kStagedThreads / SGL;
 
   for (int64_t k = 0; k < S; ++k) {
-    const bool ok = mbar_wait(&bar[k & 1], (uint32_t)((k >> 1) & 1));
+    const bool ok = mbar_wait(&bar[k & 1], (uint32_t)((k >> 1) & 1), wait_ns);
     if (!__syncthreads_and(ok)) {
       if (threadIdx.x == 0) {
         report_error(status, nullptr, SG_ERR_TIMEOUT, 0);
         // the other buffer's copies, if in flight: wait for them (bounded)
-        if (k + 1 < S) mbar_wait(&bar[(k + 1) & 1], (uint32_t)(((k + 1) >> 1) & 1));
+        if (k + 1 < S && k + 1 != skip_stage) mbar_wait(&bar[(k + 1) & 1], (uint32_t)(((k + 1) >> 1) & 1), wait_ns);
       }
       return;
     }
@@ -387,4 +397,16 @@ extern "C" int sg_spmm_staged(int dtype, int block, int64_t rows, int64_t cols, 
                                  (const double*)scale, (const double*)dshift, (const double*)y, row_mask, status,
                                  s);
   return SG_ERR_ARG;
+}
+
+// Test hook: make the stage-tiled SpMM skip the copies of one stage (so its
+// bounded wait runs out with nothing in flight) and shorten the wait limit;
+// skip_stage < 0 and wait_ns <= 0 restore normal operation.  Synchronous.
+extern "C" int sg_test_staged_fault(int skip_stage, int64_t wait_ns) {
+  const int v = skip_stage < 0 ? -1 : skip_stage;
+  const unsigned long long ns = wait_ns > 0 ? (unsigned long long)wait_ns : kWaitNs;
+  if (cudaMemcpyToSymbol(g_staged_skip_stage, &v, sizeof(v)) != cudaSuccess ||
+      cudaMemcpyToSymbol(g_staged_wait_ns, &ns, sizeof(ns)) != cudaSuccess)
+    return SG_ERR_CUDA;
+  return SG_OK;
 }

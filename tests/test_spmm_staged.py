@@ -176,3 +176,47 @@ def test_dynamic_schedule_equals_static(block, valued, shift, masked, variant):
     assert torch.equal(o1, o2)
     assert L.sg_spmm_dyn(1, block, rows, ip.data_ptr(), ix.data_ptr(), None, inp.data_ptr(), o2.data_ptr(),
                          sc.data_ptr(), None, None, 0, None, cnt.data_ptr(), sh) == _lib.SG_ERR_ARG
+
+
+@pytest.mark.gpu
+def test_staged_wait_runs_out_and_reports_timeout():
+    """Failure detection without a GPU fault: the test hook makes the kernel
+    skip the copies of stage 1, so that stage's bounded wait (shortened to
+    50 ms) runs out with nothing in flight.  The call returns, the status
+    word says SG_ERR_TIMEOUT, and once the hook is cleared the same call on
+    the same context gives the right product."""
+    import torch
+    L = _lib.lib()
+    dev = torch.device("cuda", 0)
+    rows, cols, block = 4000, 30000, 8
+    indptr, idx, _ = random_csr(rows, cols, 30, 99, False)
+    nb = int(L.sg_staged_table_bytes(0, block, rows, cols))
+    assert nb > 0
+    t = lambda a, dt: torch.from_numpy(np.ascontiguousarray(a)).to(dev, dt)  # noqa: E731
+    d_ptr, d_idx = t(indptr, torch.int64), t(idx, torch.int32)
+    inp = np.random.default_rng(1).standard_normal((cols, block))
+    d_in, d_scale = t(inp, torch.float32), torch.ones(rows, dtype=torch.float32, device=dev)
+    out = torch.zeros(rows, block, dtype=torch.float32, device=dev)
+    table = torch.empty(nb, dtype=torch.uint8, device=dev)
+    sh = torch.cuda.current_stream(dev).cuda_stream
+    assert L.sg_staged_table(0, block, rows, cols, d_ptr.data_ptr(), d_idx.data_ptr(), table.data_ptr(), nb, sh) == 0
+    st = _lib.DeviceStatus(dev)
+
+    def call():
+        return L.sg_spmm_staged(0, block, rows, cols, d_ptr.data_ptr(), d_idx.data_ptr(), None, table.data_ptr(),
+                                d_in.data_ptr(), out.data_ptr(), d_scale.data_ptr(), None, None, 0, None,
+                                st.status_ptr, sh)
+    assert L.sg_test_staged_fault(1, 50_000_000) == 0
+    try:
+        assert call() == 0
+        torch.cuda.synchronize()
+        assert int(st.buf[0].item()) == _lib.SG_ERR_TIMEOUT
+    finally:
+        assert L.sg_test_staged_fault(-1, 0) == 0
+    st.buf.zero_()
+    assert call() == 0
+    torch.cuda.synchronize()
+    assert int(st.buf[0].item()) == 0
+    X = sp.csr_matrix((np.ones(idx.size), idx, indptr), shape=(rows, cols))
+    ref = X @ inp.astype(np.float32).astype(np.float64)
+    assert np.allclose(out.cpu().numpy(), ref, rtol=2e-6, atol=2e-5 * np.abs(ref).max())
