@@ -11,8 +11,15 @@ import ast
 import json
 import os
 
+# root of the SnapATAC2 source tree the fixtures are cut from: the first
+# command-line argument, else $SNAPATAC2_REFERENCE
+import sys  # noqa: E402
+REFERENCE_ROOT = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("SNAPATAC2_REFERENCE", "")
+if not REFERENCE_ROOT:
+    sys.exit("usage: python " + os.path.basename(__file__) + " <SnapATAC2 source root> (or set SNAPATAC2_REFERENCE)")
+
 ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
-REF = "/root/reference/snapatac2-python/python/snapatac2"
+REF = os.path.join(REFERENCE_ROOT, "snapatac2-python/python/snapatac2")
 TARGETS = [("pp", "import_fragments", "preprocessing/_basic.py"),
            ("pp", "add_tile_matrix", "preprocessing/_basic.py"),
            ("pp", "make_peak_matrix", "preprocessing/_basic.py"),

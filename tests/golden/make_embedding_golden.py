@@ -28,10 +28,16 @@ import sys
 import numpy as np
 import scipy.sparse as sp
 
+# root of the SnapATAC2 source tree the fixtures are cut from: the first
+# command-line argument, else $SNAPATAC2_REFERENCE
+REFERENCE_ROOT = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("SNAPATAC2_REFERENCE", "")
+if not REFERENCE_ROOT:
+    sys.exit("usage: python " + os.path.basename(__file__) + " <SnapATAC2 source root> (or set SNAPATAC2_REFERENCE)")
+
 ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
 sys.path.insert(0, ROOT)
-REF_RS = "/root/reference/snapatac2-python/src/embedding.rs"
-REF_PY = "/root/reference/snapatac2-python/python/snapatac2/tools/_embedding.py"
+REF_RS = os.path.join(REFERENCE_ROOT, "snapatac2-python/src/embedding.rs")
+REF_PY = os.path.join(REFERENCE_ROOT, "snapatac2-python/python/snapatac2/tools/_embedding.py")
 
 
 def embedded(name: str):

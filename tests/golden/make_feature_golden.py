@@ -16,8 +16,15 @@ import os
 
 import numpy as np
 
+# root of the SnapATAC2 source tree the fixtures are cut from: the first
+# command-line argument, else $SNAPATAC2_REFERENCE
+import sys  # noqa: E402
+REFERENCE_ROOT = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("SNAPATAC2_REFERENCE", "")
+if not REFERENCE_ROOT:
+    sys.exit("usage: python " + os.path.basename(__file__) + " <SnapATAC2 source root> (or set SNAPATAC2_REFERENCE)")
+
 ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
-REF = "/root/reference/snapatac2-python/python/snapatac2/preprocessing/_basic.py"
+REF = os.path.join(REFERENCE_ROOT, "snapatac2-python/python/snapatac2/preprocessing/_basic.py")
 CASES = [  # (n features, fraction of zero counts, max count, lower, upper, total)
     (5000, 0.3, 5, 0.005, 0.005, 1000),
     (5000, 0.0, 50, 0.1, 0.0, 5000),

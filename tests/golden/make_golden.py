@@ -23,10 +23,16 @@ import sys
 
 import numpy as np
 
+# root of the SnapATAC2 source tree the fixtures are cut from: the first
+# command-line argument, else $SNAPATAC2_REFERENCE
+REFERENCE_ROOT = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("SNAPATAC2_REFERENCE", "")
+if not REFERENCE_ROOT:
+    sys.exit("usage: python " + os.path.basename(__file__) + " <SnapATAC2 source root> (or set SNAPATAC2_REFERENCE)")
+
 ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
 sys.path.insert(0, ROOT)
 OUT = os.path.join(ROOT, "tests", "golden")
-REF_GENOME_RS = "/root/reference/snapatac2-core/src/genome.rs"
+REF_GENOME_RS = os.path.join(REFERENCE_ROOT, "snapatac2-core/src/genome.rs")
 
 
 def genome_goldens() -> dict:

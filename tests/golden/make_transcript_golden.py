@@ -12,8 +12,15 @@ import json
 import os
 import re
 
+# root of the SnapATAC2 source tree the fixtures are cut from: the first
+# command-line argument, else $SNAPATAC2_REFERENCE
+import sys  # noqa: E402
+REFERENCE_ROOT = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("SNAPATAC2_REFERENCE", "")
+if not REFERENCE_ROOT:
+    sys.exit("usage: python " + os.path.basename(__file__) + " <SnapATAC2 source root> (or set SNAPATAC2_REFERENCE)")
+
 ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
-REF = "/root/reference/snapatac2-core/src/genome.rs"
+REF = os.path.join(REFERENCE_ROOT, "snapatac2-core/src/genome.rs")
 
 
 def rust_str(src: str, name: str) -> str:
