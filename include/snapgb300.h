@@ -512,6 +512,31 @@ int sg_lanczos(const sg_gram_op* op, int precision, int block, int k, uint64_t s
                sg_lanczos_info* info, int* status, void* stream);
 
 /* ------------------------------------------------------------------------ */
+/* Aggregation of an existing cell x feature matrix by regions (use_x=True  */
+/* of the peak and gene matrices) -- replaces read_chrom_values().           */
+/*   aggregate_by(counter) in create_peak_matrix / create_gene_matrix        */
+/*   (snapatac2-core/src/feature_count/matrix.rs:121-128,211-218,           */
+/*   data_iter.rs:866-891): each entry (feature j, value v) adds v to every  */
+/*   region overlapping feature j's interval (RegionCounter::insert,         */
+/*   counter.rs:95-106).  fptr/fregion: CSR of the feature -> region map     */
+/*   (region ids < n_regions).  Two calls: sg_csr_aggregate_count writes     */
+/*   eoff[n+1] (exclusive offsets of each row's expanded records, total at   */
+/*   eoff[n]); sg_csr_aggregate_run (scratch of                              */
+/*   sg_csr_aggregate_scratch_bytes(n, total) bytes, 256-byte aligned)       */
+/*   writes out_indptr[n+1], out_idx (regions ascending per row), out_val    */
+/*   (dtype 0: uint32 sums, status SG_ERR_CONVERT past 2^32-1; 1: FP64 sums  */
+/*   in X's column order) and the entry count to the host *out_nnz; it       */
+/*   synchronises its stream once; SG_ERR_CAP if cap < nnz (*out_nnz set).   */
+/* ------------------------------------------------------------------------ */
+int sg_csr_aggregate_count(int64_t n, const int64_t* indptr, const int32_t* indices, const int64_t* fptr,
+                           int64_t* eoff, void* scan_scratch, void* stream);
+int64_t sg_csr_aggregate_scratch_bytes(int64_t n, int64_t n_records);
+int sg_csr_aggregate_run(int dtype, int64_t n, const int64_t* indptr, const int32_t* indices, const void* values,
+                         const int64_t* fptr, const int32_t* fregion, int64_t n_regions, const int64_t* eoff,
+                         int64_t n_records, void* scratch, int64_t scratch_bytes, int64_t* out_indptr,
+                         int32_t* out_idx, void* out_val, int64_t cap, int64_t* out_nnz, int* status, void* stream);
+
+/* ------------------------------------------------------------------------ */
 /* Exact kNN graph -- replaces nearest_neighbour_graph                       */
 /*   (snapatac2-python/src/knn.rs:7-16 -> snapatac2-core/src/utils/knn.rs:  */
 /*   9-31, to_csr_matrix 58-78).                                             */

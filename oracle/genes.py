@@ -132,6 +132,21 @@ def gene_matrix(indptr, pos, length, chrom_names, chrom_sizes, transcripts, *, i
     regs = promoter_regions(transcripts, upstream, downstream, include_gene_body)
     ip, ix, dv, _ = org.region_counts(indptr, pos, length, chrom_names, chrom_sizes, regs, strategy=strategy,
                                       paired=paired, min_frag_size=min_frag_size, max_frag_size=max_frag_size)
+    return _by_id(ip, ix, dv, transcripts, id_type)
+
+
+def gene_matrix_from_x(X, var_names, chrom_names, transcripts, *, id_type="gene", upstream=2000, downstream=0,
+                       include_gene_body=True):
+    """``use_x=True`` of ``create_gene_matrix`` (snapatac2-core/src/feature_count/matrix.rs:211-218): X
+    aggregated by the transcripts' promoter regions (``regions.aggregate_x``), then the same transcript /
+    gene levels as the fragment path."""
+    regs = promoter_regions(transcripts, upstream, downstream, include_gene_body)
+    ip, ix, dv, _ = org.aggregate_x(X, var_names, chrom_names, regs)
+    return _by_id(ip, ix, dv, transcripts, id_type)
+
+
+def _by_id(ip, ix, dv, transcripts, id_type):
+    """Region k read as transcript k; the gene level keeps each row's maximum over a gene's transcripts."""
     if id_type == "transcript":
         return ip, ix, dv, [t["transcript_id"] for t in transcripts]
     gidx: dict = {}
@@ -148,4 +163,4 @@ def gene_matrix(indptr, pos, length, chrom_names, chrom_sizes, transcripts, *, i
             out_val.append(row[g])
         out_ptr.append(len(out_idx))
     return (np.array(out_ptr, dtype=np.int64), np.array(out_idx, dtype=np.int64),
-            np.array(out_val, dtype=np.uint32), list(gidx))
+            np.array(out_val).astype(np.uint32), list(gidx))

@@ -159,16 +159,16 @@ def make_gene_matrix(adata, gene_anno, *, inplace: bool = False, file=None, back
     """Cell-by-gene activity matrix (``_basic.py:707-800``).
 
     ``gene_anno``: a GTF / GFF3 file (or an object with ``.annotation``).
-    Same keywords and outputs as the reference; ``use_x`` and backed
-    ``file=`` output are not supported.
+    Same keywords and outputs as the reference.  ``use_x=True`` aggregates
+    the existing X by the transcripts' regions instead of counting fragments
+    (``_basic.py:715,823``), integer X only at the gene level (maximum over
+    a gene's transcripts).  Backed ``file=`` output is not supported.
     """
     from .preprocessing import _device, _fragment_arrays, read_chrom_sizes
     if id_type not in ("gene", "transcript"):
         raise ValueError("id_type must be 'transcript' or 'gene'")
     if counting_strategy not in ("fragment", "insertion", "paired-insertion"):
         raise ValueError("Counting strategy must be one of 'insertion', 'fragment', or 'paired-insertion'")
-    if use_x:
-        raise NotImplementedError("use_x=True (aggregating X by genes) is not supported")
     if file is not None:
         raise NotImplementedError("backed (file=...) output is not supported; use file=None")
     if hasattr(gene_anno, "annotation"):
@@ -178,14 +178,27 @@ def make_gene_matrix(adata, gene_anno, *, inplace: bool = False, file=None, back
                                    gene_id_key=gene_id_key)
     regs = promoter_regions(transcripts, upstream, downstream, include_gene_body)
     dev = _device(device)
-    cs = read_chrom_sizes(adata)
-    paired, indptr, pos, length = _fragment_arrays(adata)
-    rs = build_regions(regs, cs.names, dev)
-    t_len = torch.from_numpy(np.ascontiguousarray(length).view(np.int32)).to(dev) if paired else None
-    res = region_matrix(torch.from_numpy(indptr).to(dev), torch.from_numpy(pos).to(dev), t_len, cs, rs,
-                        strategy=counting_strategy if paired else "single",
-                        min_frag_size=min_frag_size if paired else None,
-                        max_frag_size=max_frag_size if paired else None)
+    if use_x:
+        from ._binning import DeviceCSR
+        from ._regions import aggregate_x
+        Y, rnames = aggregate_x(adata.X, adata.var_names, regs, dev)
+        if id_type == "gene" and Y.dtype != np.uint32:
+            raise NotImplementedError("use_x=True with id_type='gene' needs an integer X")
+        data = Y.data.view(np.int32) if Y.dtype == np.uint32 else Y.data
+        res = DeviceCSR(torch.from_numpy(Y.indptr.astype(np.int64)).to(dev),
+                        torch.from_numpy(Y.indices.astype(np.int32)).to(dev), torch.from_numpy(data).to(dev),
+                        Y.shape)
+        rs_names = rnames
+    else:
+        cs = read_chrom_sizes(adata)
+        paired, indptr, pos, length = _fragment_arrays(adata)
+        rs = build_regions(regs, cs.names, dev)
+        rs_names = rs.names
+        t_len = torch.from_numpy(np.ascontiguousarray(length).view(np.int32)).to(dev) if paired else None
+        res = region_matrix(torch.from_numpy(indptr).to(dev), torch.from_numpy(pos).to(dev), t_len, cs, rs,
+                            strategy=counting_strategy if paired else "single",
+                            min_frag_size=min_frag_size if paired else None,
+                            max_frag_size=max_frag_size if paired else None)
     if id_type == "transcript":
         names = [t["transcript_id"] for t in transcripts]
         ip, ix, dv = res.indptr, res.indices, res.data
@@ -196,11 +209,12 @@ def make_gene_matrix(adata, gene_anno, *, inplace: bool = False, file=None, back
             gidx.setdefault(t["gene_name"], len(gidx))
         names = list(gidx)
         # region k is read as transcript k (the reference's indexing; regions repeat-free)
-        region_gene = torch.tensor([gidx[transcripts[k]["gene_name"]] for k in range(len(rs.names))],
+        region_gene = torch.tensor([gidx[transcripts[k]["gene_name"]] for k in range(len(rs_names))],
                                    dtype=torch.int32, device=dev)
         ip, ix, dv = gene_max(res.indptr, res.indices, res.data, region_gene)
         var = None
-    X = sp.csr_matrix((dv.cpu().numpy().view(np.uint32), ix.cpu().numpy(), ip.cpu().numpy()),
+    dvh = dv.cpu().numpy()
+    X = sp.csr_matrix((dvh.view(np.uint32) if dvh.dtype == np.int32 else dvh, ix.cpu().numpy(), ip.cpu().numpy()),
                       shape=(res.shape[0], len(names)))
     if inplace:
         if hasattr(adata, "set_n_vars"):

@@ -108,6 +108,10 @@ SIGNATURES: dict[str, tuple] = {
     "sg_square_values": (_I32, [_I64, _P, _P, _P]),
     "sg_basis_rotate": (_I32, [_I32, _I32, _I64, _P, _I64, _I32, _P, _I64, _I32, _P, _I64, _P]),
     "sg_test_staged_fault": (_I32, [_I32, _I64]),
+    "sg_csr_aggregate_count": (_I32, [_I64, _P, _P, _P, _P, _P, _P]),
+    "sg_csr_aggregate_scratch_bytes": (_I64, [_I64, _I64]),
+    "sg_csr_aggregate_run": (_I32, [_I32, _I64, _P, _P, _P, _P, _P, _I64, _P, _I64, _P, _I64, _P, _P, _P, _I64,
+                                    _P, _P, _P]),
     "sg_sym_eig_work_bytes": (_I64, [_I32, _I32, _I32]),
     "sg_sym_eig": (_I32, [_I32, _P, _I64, _I32, _I32, _P, _P, _P, _I64, _P]),
     "sg_lanczos_work_bytes": (_I64, [_I32, _I32, _I32, _I64, _I64, _I32, _I32]),
@@ -151,7 +155,7 @@ KERNELS_PER_CALL = {
     "sg_square_values": 1,
     "sg_frag_count_lines": 4, "sg_frag_index_lines": 1, "sg_region_plan": 4, "sg_region_run": 5,
     "sg_csr_row_ptr": 4, "sg_csr_copy_rows": 1, "sg_gather_bytes": 1, "sg_nystrom_rescale": 1,
-    "sg_sym_eig": 7,
+    "sg_sym_eig": 7, "sg_csr_aggregate_count": 2, "sg_csr_aggregate_run": 14,
 }
 
 _lock = threading.Lock()

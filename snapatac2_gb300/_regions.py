@@ -8,6 +8,7 @@ Region lookup and counting run in ``csrc/region_count.cu`` behind the C ABI
 """
 from __future__ import annotations
 
+import ctypes
 import gzip
 from dataclasses import dataclass
 
@@ -138,6 +139,141 @@ def _peaks_from(adata, use_rep, peak_file):
     return list(use_rep)
 
 
+def _feature_intervals(var_names):
+    """(chrom names, chrom id per feature, start, end) of X's features: from
+    the tile layout of a tile matrix (no strings), else by parsing
+    "chrom:start-end" names (``GenomicRange::from_str``)."""
+    from .genome import TileNames
+    if isinstance(var_names, TileNames):
+        gi = var_names._index
+        counts = np.diff(np.concatenate([[0], gi.binned_accum.astype(np.int64)]))
+        cid = np.repeat(np.arange(len(gi.names), dtype=np.int64), counts)
+        first = np.repeat(np.concatenate([[0], gi.binned_accum[:-1].astype(np.int64)]), counts)
+        start = (np.arange(int(counts.sum()), dtype=np.int64) - first) * gi.step
+        end = np.minimum(start + gi.step, np.asarray(gi.sizes, dtype=np.int64)[cid])
+        return list(gi.names), cid, start, end
+    names, table, cid, start, end = [], {}, [], [], []
+    for v in var_names:
+        c, a, b = parse_region(str(v))
+        if c not in table:
+            table[c] = len(names)
+            names.append(c)
+        cid.append(table[c])
+        start.append(a)
+        end.append(b)
+    return names, np.array(cid, np.int64), np.array(start, np.int64), np.array(end, np.int64)
+
+
+def overlap_map(var_names, peaks):
+    """CSR (fptr, fregion) of feature j -> the regions overlapping its
+    interval (half-open, start < other end and end > other start), and the
+    region names in feature order (repeats dropped, first kept, as the
+    reference's interval index set)."""
+    seen, regions = set(), []
+    for p in peaks:
+        r = parse_region(p) if isinstance(p, str) else (str(p[0]), int(p[1]), int(p[2]))
+        if r not in seen:
+            seen.add(r)
+            regions.append(r)
+    cnames, fcid, fs, fe = _feature_intervals(var_names)
+    m = fs.shape[0]
+    ctab = {c: i for i, c in enumerate(cnames)}
+    pair_f, pair_r = [], []
+    by_chrom: dict = {}
+    for k, (c, a, b) in enumerate(regions):
+        if c in ctab:
+            by_chrom.setdefault(ctab[c], []).append((a, b, k))
+    order = np.argsort(fcid, kind="stable")
+    bounds = np.searchsorted(fcid[order], np.arange(len(cnames) + 1))
+    for c, lst in by_chrom.items():
+        a = np.array(lst, dtype=np.int64)
+        a = a[np.lexsort((a[:, 0],))]
+        rs, re_, rid = a[:, 0], a[:, 1], a[:, 2]
+        maxend = np.maximum.accumulate(re_)
+        feats = order[bounds[c]:bounds[c + 1]]
+        s, e = fs[feats], fe[feats]
+        hi = np.searchsorted(rs, e, side="left")        # regions starting before the feature ends
+        lo = np.searchsorted(maxend, s, side="right")   # earlier regions all end at or before its start
+        cnt = np.maximum(hi - lo, 0)
+        if cnt.sum() == 0:
+            continue
+        f_rep = np.repeat(feats, cnt)
+        cand = np.repeat(lo - np.concatenate([[0], np.cumsum(cnt)[:-1]]), cnt) + np.arange(int(cnt.sum()))
+        keep = re_[cand] > np.repeat(s, cnt)
+        pair_f.append(f_rep[keep])
+        pair_r.append(rid[cand[keep]])
+    pf = np.concatenate(pair_f) if pair_f else np.zeros(0, np.int64)
+    pr = np.concatenate(pair_r) if pair_r else np.zeros(0, np.int64)
+    o = np.lexsort((pr, pf))
+    pf, pr = pf[o], pr[o]
+    fptr = np.zeros(m + 1, dtype=np.int64)
+    np.cumsum(np.bincount(pf, minlength=m), out=fptr[1:])
+    names = [f"{c}:{a}-{b}" for c, a, b in regions]
+    return fptr, pr.astype(np.int32), names
+
+
+def aggregate_x(X, var_names, peaks, device=None):
+    """``use_x=True``: X (cells x features, CSR: scipy or DeviceCSR) summed
+    by regions on the GPU (``sg_csr_aggregate_count`` / ``_run``); the
+    overlap map is built on the host from the intervals.  Integer X gives
+    uint32 sums, floating X FP64 sums.  Returns (scipy CSR, region names)."""
+    from .preprocessing import _device
+    dev = _device(device)
+    L = _lib.lib()
+    fptr, freg, names = overlap_map(var_names, peaks)
+    if isinstance(X, DeviceCSR):
+        csr = X
+        integer = csr.data is None or not torch.is_floating_point(csr.data)
+    else:
+        Xs = sp.csr_matrix(X)
+        Xs.sort_indices()
+        integer = np.issubdtype(Xs.dtype, np.integer) or Xs.dtype == bool
+        # exact values: integer counts as uint32 bits, anything else as FP64
+        data = (np.asarray(Xs.data).astype(np.uint32).view(np.int32) if integer
+                else np.asarray(Xs.data, dtype=np.float64))
+        csr = DeviceCSR(torch.from_numpy(Xs.indptr.astype(np.int64)).to(dev),
+                        torch.from_numpy(Xs.indices.astype(np.int32)).to(dev),
+                        torch.from_numpy(np.ascontiguousarray(data)).to(dev), Xs.shape)
+    n = csr.shape[0]
+    if csr.shape[1] != fptr.shape[0] - 1:
+        raise ValueError("var_names and X have different numbers of features")
+    dtype = 0 if integer else 1
+    if csr.data is None:
+        vals = torch.ones(max(csr.nnz, 1), dtype=torch.int32 if integer else torch.float64, device=dev)
+    elif integer:
+        vals = csr.data.to(torch.int64).clamp_(0, 0xFFFFFFFF).to(torch.int32) if csr.data.dtype != torch.int32 \
+            else csr.data
+    else:
+        vals = csr.data.to(torch.float64)
+    sh = torch.cuda.current_stream(dev).cuda_stream
+    t_fptr = torch.from_numpy(fptr).to(dev)
+    t_freg = torch.from_numpy(freg if freg.size else np.zeros(1, np.int32)).to(dev)
+    eoff = torch.empty(n + 1, dtype=torch.int64, device=dev)
+    scan = torch.empty(int(L.sg_scan_scratch_bytes(n + 1)), dtype=torch.uint8, device=dev)
+    _lib.check(L.sg_csr_aggregate_count(n, csr.indptr.data_ptr(), csr.indices.data_ptr(), t_fptr.data_ptr(),
+                                        eoff.data_ptr(), scan.data_ptr(), sh), "sg_csr_aggregate_count")
+    E = int(eoff[n].item()) if n else 0
+    nb = int(L.sg_csr_aggregate_scratch_bytes(n, E))
+    work = torch.empty(nb, dtype=torch.uint8, device=dev)
+    cap = max(E, 1)
+    out_ptr = torch.empty(n + 1, dtype=torch.int64, device=dev)
+    out_idx = torch.empty(cap, dtype=torch.int32, device=dev)
+    out_val = torch.empty(cap, dtype=torch.int32 if integer else torch.float64, device=dev)
+    nnz = ctypes.c_int64(0)
+    st = _lib.DeviceStatus(dev)
+    _lib.check(L.sg_csr_aggregate_run(dtype, n, csr.indptr.data_ptr(), csr.indices.data_ptr(), vals.data_ptr(),
+                                      t_fptr.data_ptr(), t_freg.data_ptr(), len(names), eoff.data_ptr(), E,
+                                      work.data_ptr(), nb, out_ptr.data_ptr(), out_idx.data_ptr(),
+                                      out_val.data_ptr(), cap, ctypes.byref(nnz), st.status_ptr, sh),
+               "sg_csr_aggregate_run")
+    st.raise_if_error("aggregation by regions")
+    k = int(nnz.value)
+    data = out_val[:k].cpu().numpy()
+    data = data.view(np.uint32) if integer else data
+    Y = sp.csr_matrix((data, out_idx[:k].cpu().numpy(), out_ptr.cpu().numpy()), shape=(n, len(names)))
+    return Y, names
+
+
 def make_peak_matrix(adata, *, use_rep=None, inplace: bool = False, file=None, backend="hdf5", peak_file=None,
                      chunk_size: int = 500, use_x: bool = False, min_frag_size: int | None = None,
                      max_frag_size: int | None = None, counting_strategy: str = "paired-insertion",
@@ -146,18 +282,26 @@ def make_peak_matrix(adata, *, use_rep=None, inplace: bool = False, file=None, b
 
     Same keywords and outputs: a new AnnData (``X`` uint32 counts, obs
     copied, ``var_names`` "chrom:start-end") or, with ``inplace=True``,
-    ``adata.X`` / ``adata.var_names`` replaced.  ``use_x`` (aggregating an
-    existing X) and backed ``file=`` output are not supported.
+    ``adata.X`` / ``adata.var_names`` replaced.  ``use_x=True`` aggregates
+    the existing X by the peaks instead of counting fragments (``_basic.py:
+    586,704``).  Backed ``file=`` output is not supported.
     """
     from .preprocessing import _device, _fragment_arrays, read_chrom_sizes
     if counting_strategy not in ("fragment", "insertion", "paired-insertion"):
         raise ValueError("Counting strategy must be one of 'insertion', 'fragment', or 'paired-insertion'")
-    if use_x:
-        raise NotImplementedError("use_x=True (aggregating X by peaks) is not supported")
     if file is not None:
         raise NotImplementedError("backed (file=...) output is not supported; use file=None")
     peaks = _peaks_from(adata, use_rep, peak_file)
     dev = _device(device)
+    if use_x:
+        X, names = aggregate_x(adata.X, adata.var_names, peaks, dev)
+        if inplace:
+            if hasattr(adata, "set_n_vars"):
+                adata.set_n_vars(X.shape[1])
+            adata.X = X
+            adata.var_names = names
+            return None
+        return AnnData(X, obs=dict(getattr(adata, "obs", {}) or {}), obs_names=adata.obs_names, var_names=names)
     cs = read_chrom_sizes(adata)
     paired, indptr, pos, length = _fragment_arrays(adata)
     regions = build_regions(peaks, cs.names, dev)
@@ -179,4 +323,4 @@ def make_peak_matrix(adata, *, use_rep=None, inplace: bool = False, file=None, b
                    var_names=regions.names)
 
 
-__all__ = ["make_peak_matrix", "build_regions", "region_matrix", "parse_region"]
+__all__ = ["make_peak_matrix", "build_regions", "region_matrix", "parse_region", "aggregate_x", "overlap_map"]

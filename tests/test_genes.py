@@ -72,3 +72,28 @@ def test_gpu_gene_matrix_matches_oracle(tmp_path, id_type, kw):
     np.testing.assert_array_equal(X.indices, ref[1])
     np.testing.assert_array_equal(X.data, ref[2])
     assert X.dtype == np.uint32
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("id_type", ["gene", "transcript"])
+def test_gpu_use_x_gene_matrix_matches_oracle(tmp_path, id_type):
+    """make_gene_matrix(use_x=True): the tile matrix aggregated by the
+    transcripts' promoter regions (transcript level) and its maximum over
+    each gene's transcripts (gene level), against the oracle."""
+    import snapatac2_gb300 as snap
+    from oracle import binning as ob
+    from snapatac2_gb300 import synthetic as S
+    g = S.make_genome(total=20_000_000, n_chrom=6)
+    fr = S.make_fragments(25, g, median_frags=500, enriched_bins=800, seed=8)
+    p = tmp_path / "anno.gtf"
+    p.write_text(_annotation(g, np.random.default_rng(3)))
+    ad = snap.pp.fragments_to_anndata(fr.indptr, fr.pos, fr.length, g)
+    snap.pp.add_tile_matrix(ad, exclude_chroms=None)
+    got = snap.pp.make_gene_matrix(ad, str(p), id_type=id_type, use_x=True)
+    tiles = [ad.var_names[i] for i in range(ad.n_vars)]
+    ref = ogn.gene_matrix_from_x(ad.X, tiles, [c for c, _ in g], ogn.read_transcripts(p), id_type=id_type)
+    assert list(got.var_names) == ref[3]
+    X = got.X.tocsr()
+    np.testing.assert_array_equal(X.indptr, ref[0])
+    np.testing.assert_array_equal(X.indices, ref[1])
+    np.testing.assert_array_equal(X.data, ref[2].astype(np.uint32))

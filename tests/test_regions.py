@@ -218,3 +218,72 @@ def test_oracle_aggregate_x_of_tiles_is_the_insertion_peak_matrix():
     np.testing.assert_array_equal(agg[0], ref[0])
     np.testing.assert_array_equal(agg[1], ref[1])
     np.testing.assert_array_equal(agg[2], ref[2].astype(np.float64))
+
+
+# ------------------------------------------------------------ use_x -----
+def test_overlap_map_matches_brute_force_and_tile_layout():
+    """The host feature -> region map of use_x: every overlapping region of
+    every feature (half-open intervals), from parsed names and from a tile
+    matrix's layout alike."""
+    from snapatac2_gb300._regions import overlap_map
+    from snapatac2_gb300.genome import GenomeIndex, TileNames
+    rng = np.random.default_rng(0)
+    var = [f"chr{c}:{s}-{s + rng.integers(50, 800)}" for c in (1, 2) for s in rng.integers(0, 20000, 200)]
+    peaks = ([f"chr{c}:{s}-{s + rng.integers(10, 3000)}" for c in (1, 2, 3) for s in rng.integers(0, 20000, 100)]
+             + ["chr1:5-10", "chr1:5-10"])
+    fptr, freg, names = overlap_map(var, peaks)
+    regs = org.unique_regions(peaks)
+    assert names == [f"{c}:{s}-{e}" for c, s, e in regs]
+    for j, v in enumerate(var):
+        c, s, e = org.parse_region(v)
+        want = sorted(k for k, (rc, rs, re_) in enumerate(regs) if rc == c and rs < e and re_ > s)
+        assert freg[fptr[j]:fptr[j + 1]].tolist() == want
+    g = [("chr1", 12345), ("chr2", 7000), ("chrX", 999)]
+    tiles = TileNames(GenomeIndex(g, 500))
+    a = overlap_map(tiles, peaks)
+    b = overlap_map([tiles[i] for i in range(len(tiles))], peaks)
+    for x, y in zip(a[:2], b[:2]):
+        np.testing.assert_array_equal(x, y)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("integer", [True, False])
+def test_gpu_use_x_peak_matrix_matches_oracle(integer):
+    """make_peak_matrix(use_x=True) on a tile matrix: the aggregation by
+    peaks equals the oracle's restatement entry for entry (uint32 sums of
+    integer counts, FP64 sums of real values) and, for insertion counts
+    over whole-tile peaks, the insertion peak matrix of the fragments."""
+    import snapatac2_gb300 as snap
+    from oracle import binning as ob
+    g, fr, _ = _data(n_cells=40, seed=37)
+    names, sizes = [c for c, _ in g], [s for _, s in g]
+    ip, ix, dv, ncol = ob.tile_bin(fr.indptr, fr.pos, fr.length, g, bin_size=500,
+                                   counting_strategy="insertion", exclude_chroms=[])[:4]
+    tiles = [f"{c}:{s}-{min(s + 500, size)}" for c, size in g for s in range(0, size, 500)]
+    rng = np.random.default_rng(5)
+    peaks = []
+    for c, size in g:
+        for s in np.sort(rng.choice(size // 500 - 4, 60, replace=False)).tolist():
+            peaks.append(f"{c}:{s * 500}-{(s + int(rng.integers(1, 4))) * 500}")
+        peaks.append(f"{c}:{int(rng.integers(0, size // 2))}-{size // 2 + 777}")  # long, unaligned
+    vals = dv.astype(np.uint32) if integer else dv.astype(np.float64) * rng.uniform(0.5, 2.0, dv.size)
+    X = sp.csr_matrix((vals, ix, ip), shape=(fr.n_cells, ncol))
+    ad = snap.AnnData(X, var_names=tiles)
+    out = snap.pp.make_peak_matrix(ad, use_rep=peaks, use_x=True)
+    ref = org.aggregate_x(X, tiles, names, peaks)
+    Y = out.X
+    np.testing.assert_array_equal(Y.indptr, ref[0])
+    np.testing.assert_array_equal(Y.indices, ref[1])
+    if integer:
+        assert Y.dtype == np.uint32
+        np.testing.assert_array_equal(Y.data.astype(np.float64), ref[2])
+        aligned = [p for p in peaks if int(p.split(":")[1].split("-")[0]) % 500 == 0
+                   and int(p.split("-")[1]) % 500 == 0]
+        ins = org.region_counts(fr.indptr, fr.pos, fr.length, names, sizes, aligned, strategy="insertion")
+        sub = snap.pp.make_peak_matrix(ad, use_rep=aligned, use_x=True).X
+        np.testing.assert_array_equal(sub.indptr, ins[0])
+        np.testing.assert_array_equal(sub.data, ins[2])
+    else:
+        assert Y.dtype == np.float64
+        np.testing.assert_allclose(Y.data, ref[2], rtol=1e-15, atol=0)
+    assert list(out.var_names) == ref[3]
