@@ -57,12 +57,10 @@ def test_peak_and_gene_matrix_arguments(tmp_path):
     ad = _adata()
     with pytest.raises(ValueError, match="Counting strategy must be one of"):
         snap.pp.make_peak_matrix(ad, use_rep=["chr1:0-10"], counting_strategy="bogus")
-    with pytest.raises(NotImplementedError, match="use_x"):
-        snap.pp.make_peak_matrix(ad, use_rep=["chr1:0-10"], use_x=True)
     with pytest.raises(ValueError, match="id_type must be 'transcript' or 'gene'"):
         snap.pp.make_gene_matrix(ad, str(tmp_path / "a.gtf"), id_type="bogus")
-    with pytest.raises(NotImplementedError, match="use_x"):
-        snap.pp.make_gene_matrix(ad, str(tmp_path / "a.gtf"), use_x=True)
+    with pytest.raises(NotImplementedError, match="backed"):
+        snap.pp.make_peak_matrix(ad, use_rep=["chr1:0-10"], use_x=True, file="out.h5ad")
 
 
 def test_import_fragments_arguments(tmp_path):
