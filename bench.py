@@ -439,7 +439,7 @@ def large_stage(args, dev):
     return {"workload": f"{n} cells x {m} features, ~{int(args.nnz)} nnz/cell binary CSR (nnz={csr.nnz}), "
                         f"spectral n_comps={args.ncomps} (mixed) + exact kNN k=50; CSR resident in HBM",
             "target_wall_s": 30, "autotuned_block": auto,
-            "block_choice_predicted_ms": _block_prediction(op, args.ncomps), **runs,
+            "block_choice_predicted_ms": _block_prediction(n, m, csr.nnz, args.ncomps), **runs,
             "accuracy_vs_fp64_gpu": {**acc, "compared_block": b, "fp64_form_s": t64,
                                      "fp64_block_matvecs": res64.info["block_matvecs"]},
             "max_residual_rel": float(np.max(r) / anorm),
@@ -447,10 +447,11 @@ def large_stage(args, dev):
             "knn_checked_rows": checked, "knn_sample_identical_to_oracle": same, "clocks": clk}
 
 
-def _block_prediction(op, k, precision="mixed"):
-    """The block autotuner's predicted seconds per candidate for this shape."""
+def _block_prediction(n, m, nnz, k, precision="mixed"):
+    """The block autotuner's predicted milliseconds per candidate block for
+    this shape class (None when the block was given)."""
     from snapatac2_gb300 import _eigen
-    got = _eigen._BLOCK_CHOICE.get(_eigen._shape_class(op, _eigen._DT[precision][0], k))
+    got = _eigen._BLOCK_CHOICE.get((_eigen._DT[precision][0], n, m, nnz >> 20, False, k))
     return {str(b): round(v, 3) for b, v in got[1].items()} if got else None
 
 
@@ -740,6 +741,7 @@ def run_gpu(args):
                                f"(nnz={nnz}), n_comps={args.ncomps}, mixed precision",
                    "parallelism": "replicas" if world > 1 else "single GPU", "block": info["block"],
                    "block_choice": "given" if args.block else "autotuned (choose_block)",
+                   "block_choice_predicted_ms": _block_prediction(n, m, nnz, args.ncomps),
                    "l2": "inputs larger than L2 (CSR indices 4 B x nnz)",
                    "block_matvecs": info["block_matvecs"], "restarts": info["restarts"], "basis": info["basis"],
                    "phase_seconds": info.get("phase_seconds")},

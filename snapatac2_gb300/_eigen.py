@@ -544,10 +544,42 @@ def _ritz_ms(M: int, keep: int, stream: int) -> float:
     return _RITZ_MS[M]
 
 
+def _quick_variants(op: GramOperator, code: int, b: int, Z, Zs, T, W, stream: int) -> tuple[int, int]:
+    """Fastest of a few SpMM kernels per pass (one warm and one timed launch
+    each): the kernels the full tuner picks most often, so that the block
+    choice compares blocks at near-tuned speed without the full search."""
+    if code == 0:
+        cands = ([DYN + 7, DYN + 5, DYN + 1, 6, 2], [6, 2, DYN + 2, DYN + 6])
+    else:
+        cands = ([0, 1, 4, 5], [0, 1, 4, 5])
+    best = []
+    for which, cs in enumerate(cands):
+        times = []
+        for v in cs:
+            def launch():
+                if which == 0:
+                    op.spmm_pass(0, v, code, b, Zs, T, stream)
+                else:
+                    op.spmm_pass(1, v, code, b, T, W, stream, Z)
+            try:
+                launch()
+            except _lib.SnapGB300Error:
+                times.append(math.inf)
+                continue
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            launch()
+            e1.record()
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+        best.append(cs[int(np.argmin(times))])
+    return best[0], best[1]
+
+
 def _block_step_ms(op: GramOperator, code: int, b: int, ncols: int, ld: int, stream: int) -> float:
-    """CUDA-event time of one block step at block b: the operator with the
-    default SpMM kernels, two Gram-Schmidt passes against ncols basis
-    vectors, two Cholesky-QR passes (scratch operands)."""
+    """CUDA-event time of one block step at block b: the operator with
+    quick-tuned SpMM kernels (``_quick_variants``), two Gram-Schmidt passes
+    against ncols basis vectors, two Cholesky-QR passes (scratch operands)."""
     L = _lib.load()
     dev = op.a.device
     tdt = torch.float32 if code == 0 else torch.float64
@@ -562,7 +594,7 @@ def _block_step_ms(op: GramOperator, code: int, b: int, ncols: int, ld: int, str
     st = _lib.DeviceStatus(dev)
     for t in (Q, Z, Zs, W):
         _lib.check(L.sg_fill_random(code, t.numel(), 7, t.data_ptr(), stream), "fill")
-    vt, vx = (DYN + 7, 6) if code == 0 else (1, 1)
+    vt, vx = _quick_variants(op, code, b, Z, Zs, T, W, stream)
 
     def step():
         op.spmm_pass(0, vt, code, b, Zs, T, stream)
@@ -594,8 +626,9 @@ def choose_block(op: GramOperator, k: int, precision: str = "mixed", stream: int
     with V(b) the vector matvecs the solve needs: the observed count of an
     earlier solve of this shape class at block b, else BLOCK_PRIOR scaled by
     the observed counts at other blocks.  Block steps are timed on scratch
-    operands with the default SpMM kernels (the kernels are tuned afterwards
-    for the chosen block only: tuning every block costs seconds at 1M cells).
+    operands with quick-tuned SpMM kernels (the full kernel search runs
+    afterwards for the chosen block only: searching every block costs
+    seconds at 1M cells).
     """
     code = _DT[precision][0]
     key = _shape_class(op, code, k)

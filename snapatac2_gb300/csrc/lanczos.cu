@@ -56,7 +56,7 @@ proj_partial(int64_t n, const T* __restrict__ Q, int64_t ldq, int ncols, const T
       const int p = threadIdx.x + q * kProjBlock;
       if (p < ncols) {
         // several rows' loads in flight, then their FMAs in row order
-        constexpr int RU = B * CPT * (int)sizeof(T) >= 64 ? 2 : 8;
+        constexpr int RU = sizeof(T) == 8 ? (B * CPT >= 8 ? 2 : 8) : (B * CPT >= 32 ? 4 : 8);
         for (int i0 = 0; i0 < nr; i0 += RU) {
           T qv[RU];
 #pragma unroll
@@ -194,8 +194,19 @@ update_kernel(int64_t n, const T* __restrict__ Q, int64_t ldq, int ncols, const 
       for (int u = 0; u < 8; ++u) {
         const int p = p0 + u * 32 + lane;
         if (p < ncols) {
+          // C's row p read as 16-byte vectors: word-wise reads at a B-word
+          // stride put several lanes on one shared-memory bank; the FMAs
+          // and their order are unchanged
+          using VT = typename V16<T>::type;
+          constexpr int VW = V16<T>::n;
+          const VT* cv = reinterpret_cast<const VT*>(cs + (size_t)p * B);
 #pragma unroll
-          for (int c = 0; c < B; ++c) acc[c] = fma(qv[u], cs[p * B + c], acc[c]);
+          for (int j = 0; j < B / VW; ++j) {
+            const VT c4 = cv[j];
+            const T* cc = reinterpret_cast<const T*>(&c4);
+#pragma unroll
+            for (int q = 0; q < VW; ++q) acc[j * VW + q] = fma(qv[u], cc[q], acc[j * VW + q]);
+          }
         }
       }
     }
