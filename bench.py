@@ -541,7 +541,7 @@ def gather_ceiling(csr, block, dev):
     del op
     rows_per_s = 2 * nnz / ((gt + gx) / 1e3)
     return {"what": "row gathers of each SpMM pass alone over the same index streams (sg_gather_ceiling): "
-                    "one L1/L2 line per gathered row at block 8 FP32",
+                    f"one gathered row of {block} FP32 values per nonzero",
             "xt_gather_ms": gt, "x_gather_ms": gx, "gathered_rows_per_s": rows_per_s,
             "gathered_GBps": rows_per_s * block * 4 / 1e9}
 
@@ -620,10 +620,11 @@ def run_gpu(args):
         n_apply += napp
     n_launch = 2 * n_apply
     spmm_ms = (t_time + x_time) / max(n_launch, 1)
-    # DRAM traffic per launch: ncu dram__bytes_read.sum + dram__bytes_write.sum of both passes at
-    # 20,000 cells x 500,000 features came to 0.997 (Xᵀ pass) and 1.005 (X pass) of the algorithmic
-    # bytes; both grow with nnz, so the 100k launch is scaled from its own algorithmic bytes
-    traffic = (0.997 * tb + 1.005 * xb) / max(n_launch, 1)
+    # DRAM traffic per launch: ncu dram__bytes_read.sum + dram__bytes_write.sum of the two kernels
+    # the bench runs (block 16, dynamic schedule) at 20,000 cells x 500,000 features came to 0.989
+    # (Xᵀ pass) and 1.041 (X pass) of the algorithmic bytes; both grow with nnz, so each launch here
+    # is scaled from its own algorithmic bytes
+    traffic = (0.989 * tb + 1.041 * xb) / max(n_launch, 1)
     achieved = (tb + xb) / max((t_time + x_time) / 1e3, 1e-12) / 1e9
     peak, peak_kind = peaks()
     spmm_share = (t_time + x_time) / (ms * args.steps)
@@ -741,6 +742,7 @@ def run_gpu(args):
                                f"(nnz={nnz}), n_comps={args.ncomps}, mixed precision",
                    "parallelism": "replicas" if world > 1 else "single GPU", "block": info["block"],
                    "block_choice": "given" if args.block else "autotuned (choose_block)",
+                   "spmm_variants": infos[-1].get("spmm_variants"),
                    "block_choice_predicted_ms": _block_prediction(n, m, nnz, args.ncomps),
                    "l2": "inputs larger than L2 (CSR indices 4 B x nnz)",
                    "block_matvecs": info["block_matvecs"], "restarts": info["restarts"], "basis": info["basis"],
@@ -753,7 +755,7 @@ def run_gpu(args):
         "roofline": {"kernel": "spmm_kernel (Gram matvec, Xᵀ gather over CSC + X gather over CSR)",
                      "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_kind,
-                     "traffic": traffic, "traffic_unit": "bytes per launch (ncu at 20k cells, scaled by nnz)",
+                     "traffic": traffic, "traffic_unit": "bytes per launch (ncu at 20k cells, block 16, scaled by each launch's algorithmic bytes)",
                      "launches": n_launch, "avg_launch_ms": spmm_ms,
                      "bytes_per_block_matvec": int((tb + xb) / max(n_apply, 1)),
                      "share_of_step": spmm_share},
