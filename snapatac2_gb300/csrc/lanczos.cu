@@ -14,6 +14,8 @@
 //   finish  Q[:, col:col+B] = W, Z = W, Zs = a ⊙ W
 //   hblock  Rayleigh-quotient diagonal block and coupling R into H (FP64)
 //   rotate  out = Q[:, :m] Y                (thick restart, Ritz vectors)
+#include <mutex>
+
 #include "common.cuh"
 #include "internal.h"
 
@@ -227,6 +229,263 @@ update_kernel(int64_t n, const T* __restrict__ Q, int64_t ldq, int ncols, const 
   }
 }
 
+// ---- FP32 tiled forms of proj and update -----------------------------------
+// The basis is read in stages of 32 columns (128 bytes of a row) by
+// cp.async into per-warp shared-memory rings; rows of a staged tile are
+// padded to 36 floats, so the 16-byte reads of eight consecutive rows touch
+// 32 distinct banks.  Columns past ncols and rows past the limit are
+// zero-filled by the copy itself (src-size < 16), so the inner loops have no
+// bounds tests.  Only used when Q, W and every row start are 16-byte aligned.
+constexpr int kStageCols = 32;
+constexpr int kPitch = kStageCols + 4;
+constexpr int kTileWarps = 4;
+
+__device__ __forceinline__ void cp_async16(void* dst, const void* src, int src_bytes) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_u32(dst)), "l"(src), "r"(src_bytes)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// rows [row0, row0 + R) x columns [col0, col0 + 32) of Q into buf (R x kPitch);
+// rows at or past rlim and columns at or past ncols read as zero
+template <int R>
+__device__ __forceinline__ void stage_q(float* buf, const float* __restrict__ Q, int64_t ldq, int64_t rlim,
+                                        int ncols, int64_t row0, int col0, int lane) {
+#pragma unroll
+  for (int j = 0; j < R / 4; ++j) {
+    const int idx = j * 32 + lane;
+    const int r = idx >> 3, c = (idx & 7) * 4;
+    const int64_t row = row0 + r;
+    const int col = col0 + c;
+    int bytes = (ncols - col) * 4;
+    bytes = bytes < 0 ? 0 : (bytes > 16 ? 16 : bytes);
+    if (row >= rlim) bytes = 0;
+    cp_async16(buf + r * kPitch + c, bytes ? Q + row * ldq + col : Q, bytes);
+  }
+}
+
+// W -= Q[:, :ncols] C.  Each warp owns 64-row tiles (rows lane and lane + 32
+// of a tile per lane, all B columns in registers); C (FP32, zero past ncols)
+// sits in shared memory and is read as broadcasts.  The warp walks (tile,
+// stage) in order with a two-deep cp.async ring.  Each row's sum runs over
+// the columns in ascending order: deterministic.
+template <int B>
+__global__ void __launch_bounds__(kTileWarps * 32)
+update_tiled(int64_t n, const float* __restrict__ Q, int64_t ldq, int ncols, const double* __restrict__ C,
+             float* __restrict__ W) {
+  constexpr int R = 64;
+  extern __shared__ __align__(16) unsigned char sraw[];
+  const int nch = (ncols + kStageCols - 1) / kStageCols;
+  float* cs = reinterpret_cast<float*>(sraw);
+  float* ring = cs + (size_t)nch * kStageCols * B;
+  for (int t = threadIdx.x; t < nch * kStageCols * B; t += blockDim.x) cs[t] = t < ncols * B ? (float)C[t] : 0.f;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  float* buf = ring + (size_t)wid * 2 * R * kPitch;
+  const int64_t ntiles = (n + R - 1) / R;
+  const int64_t nw = (int64_t)gridDim.x * kTileWarps;
+  int64_t tile = blockIdx.x * (int64_t)kTileWarps + wid;
+  if (tile >= ntiles) return;
+  int ch = 0, sl = 0;
+  stage_q<R>(buf, Q, ldq, n, ncols, tile * R, 0, lane);
+  cp_async_commit();
+  float a0[B], a1[B];
+#pragma unroll
+  for (int c = 0; c < B; ++c) a0[c] = a1[c] = 0.f;
+  while (true) {
+    int64_t ntile = tile;
+    int nchk = ch + 1;
+    if (nchk == nch) {
+      nchk = 0;
+      ntile = tile + nw;
+    }
+    const bool more = ntile < ntiles;
+    if (more) stage_q<R>(buf + (sl ^ 1) * R * kPitch, Q, ldq, n, ncols, ntile * R, nchk * kStageCols, lane);
+    cp_async_commit();
+    cp_async_wait<1>();
+    __syncwarp();
+    const float* qb = buf + sl * R * kPitch;
+    const float* cst = cs + (size_t)ch * kStageCols * B;
+#pragma unroll 2
+    for (int p4 = 0; p4 < kStageCols / 4; ++p4) {
+      const float4 qa = *reinterpret_cast<const float4*>(qb + lane * kPitch + 4 * p4);
+      const float4 qc = *reinterpret_cast<const float4*>(qb + (lane + 32) * kPitch + 4 * p4);
+      const float va[4] = {qa.x, qa.y, qa.z, qa.w}, vc[4] = {qc.x, qc.y, qc.z, qc.w};
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const float4* cv = reinterpret_cast<const float4*>(cst + (4 * p4 + q) * B);
+#pragma unroll
+        for (int j = 0; j < B / 4; ++j) {
+          const float4 c4 = cv[j];
+          a0[4 * j + 0] = fmaf(va[q], c4.x, a0[4 * j + 0]);
+          a0[4 * j + 1] = fmaf(va[q], c4.y, a0[4 * j + 1]);
+          a0[4 * j + 2] = fmaf(va[q], c4.z, a0[4 * j + 2]);
+          a0[4 * j + 3] = fmaf(va[q], c4.w, a0[4 * j + 3]);
+          a1[4 * j + 0] = fmaf(vc[q], c4.x, a1[4 * j + 0]);
+          a1[4 * j + 1] = fmaf(vc[q], c4.y, a1[4 * j + 1]);
+          a1[4 * j + 2] = fmaf(vc[q], c4.z, a1[4 * j + 2]);
+          a1[4 * j + 3] = fmaf(vc[q], c4.w, a1[4 * j + 3]);
+        }
+      }
+    }
+    __syncwarp();
+    if (ch == nch - 1) {
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int64_t row = tile * R + lane + 32 * h;
+        if (row < n) {
+          float4* wr = reinterpret_cast<float4*>(W + row * B);
+#pragma unroll
+          for (int j = 0; j < B / 4; ++j) {
+            float4 v = wr[j];
+            const float* a = h ? a1 : a0;
+            v.x -= a[4 * j + 0];
+            v.y -= a[4 * j + 1];
+            v.z -= a[4 * j + 2];
+            v.w -= a[4 * j + 3];
+            wr[j] = v;
+          }
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < B; ++c) a0[c] = a1[c] = 0.f;
+    }
+    if (!more) break;
+    tile = ntile;
+    ch = nchk;
+    sl ^= 1;
+  }
+  cp_async_wait<0>();
+}
+
+// part[blk][p][c] = sum over the CTA's rows [r0, r1) of Q[i,p] W[i,c].  Per
+// stage of 32 columns the warps take the CTA's 32-row tiles in turn; a lane
+// owns 4 columns p x B/4 columns c (lane = 8 column groups x 4 output
+// groups), so per row it reads one 16-byte vector of Q and B/4 values of W.
+// The four warps' FP32 sums are added in FP64 in warp order: deterministic.
+template <int B>
+__host__ __device__ constexpr int proj_stages() {
+  return B >= 32 ? 2 : 3;
+}
+
+template <int B>
+__global__ void __launch_bounds__(kTileWarps * 32)
+proj_tiled(int64_t n, const float* __restrict__ Q, int64_t ldq, int ncols, const float* __restrict__ W,
+           double* __restrict__ part) {
+  constexpr int R = 32, CW = B / 4, kProjStages = proj_stages<B>();
+  extern __shared__ __align__(16) unsigned char sraw[];
+  double* red = reinterpret_cast<double*>(sraw);                           // [warps][32 * B]
+  float* qring = reinterpret_cast<float*>(red + kTileWarps * kStageCols * B);  // [warps][stages][R][kPitch]
+  float* wring = qring + kTileWarps * kProjStages * R * kPitch;            // [warps][stages][R][B]
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int pg = lane >> 2, cg = lane & 3;
+  const int nb = gridDim.x, b = blockIdx.x;
+  const int64_t r0 = n * b / nb, r1 = n * (b + 1) / nb;
+  const int ntc = (int)((r1 - r0 + R - 1) / R);
+  const int ntw = ntc > wid ? (ntc - wid + kTileWarps - 1) / kTileWarps : 0;
+  const int nch = (ncols + kStageCols - 1) / kStageCols;
+  const int total = ntw * nch;
+  float* qb = qring + (size_t)wid * kProjStages * R * kPitch;
+  float* wb = wring + (size_t)wid * kProjStages * R * B;
+  auto stage = [&](int i) {
+    const int ch = i / ntw, j = i % ntw;
+    const int64_t row0 = r0 + (int64_t)(wid + kTileWarps * j) * R;
+    const int sl = i % kProjStages;
+    stage_q<R>(qb + sl * R * kPitch, Q, ldq, r1, ncols, row0, ch * kStageCols, lane);
+#pragma unroll
+    for (int t = lane; t < R * CW; t += 32) {
+      const int r = t / CW, c = (t % CW) * 4;
+      const int64_t row = row0 + r;
+      const int bytes = row < r1 ? 16 : 0;
+      cp_async16(wb + (sl * R + r) * B + c, bytes ? W + row * B + c : W, bytes);
+    }
+  };
+#pragma unroll
+  for (int i = 0; i < kProjStages - 1; ++i) {
+    if (i < total) stage(i);
+    cp_async_commit();
+  }
+  int i = 0;
+  for (int ch = 0; ch < nch; ++ch) {
+    float acc[4][CW];
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+      for (int c = 0; c < CW; ++c) acc[u][c] = 0.f;
+    for (int j = 0; j < ntw; ++j, ++i) {
+      if (i + kProjStages - 1 < total) stage(i + kProjStages - 1);
+      cp_async_commit();
+      cp_async_wait<kProjStages - 1>();
+      __syncwarp();
+      const int sl = i % kProjStages;
+      const float* qs = qb + sl * R * kPitch + pg * 4;
+      const float* ws = wb + sl * R * B + cg * CW;
+#pragma unroll 4
+      for (int r = 0; r < R; ++r) {
+        const float4 q4 = *reinterpret_cast<const float4*>(qs + r * kPitch);
+        const float qv[4] = {q4.x, q4.y, q4.z, q4.w};
+        float wv[CW];
+        if constexpr (CW % 4 == 0) {
+#pragma unroll
+          for (int c = 0; c < CW; c += 4) {
+            const float4 w4 = *reinterpret_cast<const float4*>(ws + r * B + c);
+            wv[c] = w4.x;
+            wv[c + 1] = w4.y;
+            wv[c + 2] = w4.z;
+            wv[c + 3] = w4.w;
+          }
+        } else if constexpr (CW == 2) {
+          const float2 w2 = *reinterpret_cast<const float2*>(ws + r * B);
+          wv[0] = w2.x;
+          wv[1] = w2.y;
+        } else {
+          wv[0] = ws[r * B];
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+          for (int c = 0; c < CW; ++c) acc[u][c] = fmaf(qv[u], wv[c], acc[u][c]);
+      }
+      __syncwarp();
+    }
+    double* rw = red + (size_t)wid * kStageCols * B;
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+      for (int c = 0; c < CW; ++c) rw[(pg * 4 + u) * B + cg * CW + c] = (double)acc[u][c];
+    __syncthreads();
+    for (int t = threadIdx.x; t < kStageCols * B; t += blockDim.x) {
+      const int p = ch * kStageCols + t / B;
+      if (p < ncols) {
+        double s = red[t];
+#pragma unroll
+        for (int w2 = 1; w2 < kTileWarps; ++w2) s += red[(size_t)w2 * kStageCols * B + t];
+        part[((int64_t)b * ncols + p) * B + t % B] = s;
+      }
+    }
+    __syncthreads();
+  }
+  cp_async_wait<0>();
+}
+
+size_t update_tiled_smem(int B, int ncols) {
+  const int nch = (ncols + kStageCols - 1) / kStageCols;
+  return (size_t)nch * kStageCols * B * 4 + (size_t)kTileWarps * 2 * 64 * kPitch * 4;
+}
+
+template <int B>
+size_t proj_tiled_smem() {
+  return (size_t)kTileWarps * kStageCols * B * 8 + (size_t)kTileWarps * proj_stages<B>() * 32 * (kPitch + B) * 4;
+}
+
+bool tiled_ok(const void* Q, int64_t ldq, const void* W) {
+  return ((uintptr_t)Q & 15u) == 0 && ((uintptr_t)W & 15u) == 0 && (ldq & 3) == 0;
+}
+
 // Cholesky of the B x B Gram matrix (one warp, lane j owns column j):
 // G = RᵀR with R upper triangular; also Rinv = R⁻¹.  A non-positive pivot
 // relative to the diagonal sets SG_ERR_NUMERIC (rank-deficient block).  G is
@@ -402,9 +661,33 @@ __global__ void fill_random(int64_t count, uint64_t seed, T* __restrict__ out) {
   }
 }
 
+// largest dynamic shared memory of the tiled kernels (ncols <= 640, B = 32),
+// the fixed cap set on them
+constexpr int kTiledSmemCap = 200 * 1024;
+
+template <int B>
+int proj_tiled_launch(int64_t n, const float* Q, int64_t ldq, int ncols, const float* W, double* part, int nparts,
+                      double* C, cudaStream_t s) {
+  const size_t smem = proj_tiled_smem<B>();
+  static std::once_flag once;
+  static cudaError_t attr = cudaSuccess;
+  std::call_once(once, [&] {
+    attr = cudaFuncSetAttribute(proj_tiled<B>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTiledSmemCap);
+  });
+  if (attr != cudaSuccess) return SG_ERR_CUDA;
+  proj_tiled<B><<<nparts, kTileWarps * 32, smem, s>>>(n, Q, ldq, ncols, W, part);
+  SG_CHECK_LAUNCH();
+  proj_reduce<<<(ncols * B + 31) / 32, kReduceWarps * 32, 0, s>>>(nparts, ncols, B, part, C);
+  SG_CHECK_LAUNCH();
+  return SG_OK;
+}
+
 template <typename T, int B>
 int proj_t(int64_t n, const T* Q, int64_t ldq, int ncols, const T* W, double* part, int nparts, double* C,
            cudaStream_t s) {
+  if constexpr (sizeof(T) == 4) {
+    if (tiled_ok(Q, ldq, W)) return proj_tiled_launch<B>(n, Q, ldq, ncols, W, part, nparts, C, s);
+  }
   // column slices of at most 2 * kProjBlock basis vectors per launch (one
   // slice per thread column when a row of W is 128 bytes or more: two would
   // not fit the register file)
@@ -437,8 +720,43 @@ int proj_dispatch(int B, int64_t n, const T* Q, int64_t ldq, int ncols, const T*
   }
 }
 
+template <int B>
+int update_tiled_launch(int64_t n, const float* Q, int64_t ldq, int ncols, const double* C, float* W,
+                        cudaStream_t s) {
+  const size_t smem = update_tiled_smem(B, ncols);
+  if (smem > (size_t)kTiledSmemCap) return SG_ERR_ARG;
+  static std::once_flag once;
+  static cudaError_t attr = cudaSuccess;
+  std::call_once(once, [&] {
+    attr = cudaFuncSetAttribute(update_tiled<B>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTiledSmemCap);
+  });
+  if (attr != cudaSuccess) return SG_ERR_CUDA;
+  int occ = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, update_tiled<B>, kTileWarps * 32, smem) != cudaSuccess)
+    return SG_ERR_CUDA;
+  const int per_sm = occ > 0 ? occ : 1;
+  const int64_t tiles = (n + 63) / 64;
+  const int64_t want = (tiles + kTileWarps - 1) / kTileWarps;
+  const int64_t cap = (int64_t)per_sm * sm_count_l();
+  const int grid = (int)(want < cap ? want : cap);
+  update_tiled<B><<<grid, kTileWarps * 32, smem, s>>>(n, Q, ldq, ncols, C, W);
+  SG_CHECK_LAUNCH();
+  return SG_OK;
+}
+
 template <typename T>
 int update_dispatch(int B, int64_t n, const T* Q, int64_t ldq, int ncols, const double* C, T* W, cudaStream_t s) {
+  if constexpr (sizeof(T) == 4) {
+    if (tiled_ok(Q, ldq, W)) {
+      switch (B) {
+        case 4: return update_tiled_launch<4>(n, Q, ldq, ncols, C, W, s);
+        case 8: return update_tiled_launch<8>(n, Q, ldq, ncols, C, W, s);
+        case 16: return update_tiled_launch<16>(n, Q, ldq, ncols, C, W, s);
+        case 32: return update_tiled_launch<32>(n, Q, ldq, ncols, C, W, s);
+        default: return SG_ERR_ARG;
+      }
+    }
+  }
   const int grid = grid_for(n * 32, 256, 8 * sm_count_l());
   const size_t smem = (size_t)ncols * B * sizeof(T);
   if (smem > 200 * 1024) return SG_ERR_ARG;
