@@ -377,6 +377,27 @@ int sg_spmm_staged(int dtype, int block, int64_t rows, int64_t cols, const int64
                    const void* dshift, const void* y, int variant, const unsigned char* row_mask, int* status,
                    void* stream);
 
+/* Compensated-FP32 SpMM over 32 columns, used by the FP64 correction sweep */
+/* of sg_lanczos (the Gram matvec of embedding.rs:133-152 applied once to   */
+/* the Ritz vectors).  Operands are FP32 pairs (hi, lo) whose sum is the    */
+/* FP64 value (sg_ds_split); sums are carried as an FP32 value and an FP32  */
+/* compensation updated by Knuth's TwoSum, within about k * 2^-48 of the    */
+/* sum of |terms| for k terms.  `in` is rows' cols x 32 pairs (256 B a row). */
+/* pass 0: out = pairs of scale ⊙ (M in)              (dshift must be NULL) */
+/* pass 1: out = scale ⊙ (M in) - dshift ⊙ y, FP64 x 32 (y FP64, rows x 32)  */
+/* M is the CSR (ptr, idx, val; val NULL: all ones).  in, out, y 16-byte    */
+/* aligned; out must not alias in.  Variants 0-3: one or two 32-index       */
+/* chunks in flight (bit 0), static or counter-driven row schedule (bit 1,  */
+/* needs `counter`, zeroed by the call).  Deterministic.  No reference      */
+/* counterpart (an arithmetic form of the FP64 matvec).                     */
+int sg_spmm_ds_variants(void);
+int sg_spmm_ds(int pass, int64_t rows, const int64_t* ptr, const int32_t* idx, const float* val, const void* in,
+               void* out, const double* scale, const double* dshift, const double* y, int variant,
+               unsigned int* counter, void* stream);
+/* out[r, c] = (hi, lo) pair of a[r] * U[r, c] (a NULL: of U[r, c]); U is   */
+/* n x 32 FP64, out n x 32 pairs of FP32 (hi = fl32(v), lo = fl32(v - hi)). */
+int sg_ds_split(int64_t n, const double* a, const double* U, void* out, void* stream);
+
 /* Diagnostic (no reference counterpart): the row gathers of one SpMM pass  */
 /* alone -- table[idx[e]] (block values per row, same 16-byte vectors and    */
 /* lanes per row as the SpMM) for every e < nnz, folded into registers, no   */
@@ -468,12 +489,16 @@ typedef struct sg_lanczos_opts {
   int vec_positive_only;    /* 1: vectors returned for θ > 0 only (as        */
                             /* weighted_by_sd keeps), others need tol_val    */
   int max_restarts;         /* < 0: default 200 (0: no restart)              */
-  int refine;               /* mixed form: final FP64 correction sweep       */
+  int refine;               /* mixed form: final correction sweep (FP64-    */
+                            /* class AU, Rayleigh-Ritz in FP64): 1 with the  */
+                            /* compensated FP32 kernels (sg_spmm_ds), 2 with */
+                            /* FP64 kernels, 0 none                          */
   int variant_t, variant_x; /* SpMM kernel per pass (codes: < 100 gather,    */
                             /* 100 + v stage-tiled, 200 + v dynamic); -1:    */
                             /* library default                               */
-  int refine_variant_t, refine_variant_x; /* FP64 block-32 SpMM of the sweep */
-                            /* (gather or dynamic codes only)                */
+  int refine_variant_t, refine_variant_x; /* SpMM of the sweep: refine 1,  */
+                            /* sg_spmm_ds variants 0-3; refine 2, FP64      */
+                            /* block-32 gather or dynamic codes; -1 default  */
   int time_spmm;            /* 1: CUDA-event time of every SpMM launch       */
 } sg_lanczos_opts;
 

@@ -441,7 +441,7 @@ def eigsh_lm(op: GramOperator, k: int, *, precision: str = "mixed", block: int |
     t0 = time.perf_counter()
     vt, vx = _spmm_choice(op, code, block, sh)
     do_refine = bool(refine and precision == "mixed" and k <= 32)
-    rvt, rvx = _spmm_choice(op, 1, 32, sh, staged=False) if do_refine else (-1, -1)
+    rvt, rvx = -1, -1  # the sweep's compensated FP32 kernels: library defaults
     nbytes = int(L.sg_lanczos_work_bytes(code, block, k, n, op.m, M, keep))
     if nbytes <= 0:
         raise ValueError("sg_lanczos: unsupported shape")

@@ -433,8 +433,12 @@ extern "C" int sg_lanczos(const sg_gram_op* op, int precision, int block, int k,
   const int max_restarts = o.max_restarts >= 0 ? o.max_restarts : 200;
   const int vt = o.variant_t >= 0 ? o.variant_t : default_variant(code, 0);
   const int vx = o.variant_x >= 0 ? o.variant_x : default_variant(code, 1);
-  const int rvt = o.refine_variant_t >= 0 ? o.refine_variant_t : default_variant(1, 0);
-  const int rvx = o.refine_variant_x >= 0 ? o.refine_variant_x : default_variant(1, 1);
+  // correction sweep: refine 1 = compensated FP32 kernels (variants of sg_spmm_ds; dynamic rows and
+  // two index chunks for the skewed feature rows, static for the cells), 2 = FP64 kernels
+  const bool ds_sweep = o.refine != 2;
+  const int rvt = o.refine_variant_t >= 0 ? o.refine_variant_t : (ds_sweep ? 3 : default_variant(1, 0));
+  const int rvx = o.refine_variant_x >= 0 ? o.refine_variant_x : (ds_sweep ? 1 : default_variant(1, 1));
+  if (ds_sweep && (rvt > 3 || rvx > 3)) return SG_ERR_ARG;
   Basis bs = default_basis(k, b);
   int M = o.basis > 0 ? o.basis : bs.M;
   int keep = o.keep > 0 ? o.keep : bs.keep;
@@ -558,8 +562,18 @@ extern "C" int sg_lanczos(const sg_gram_op* op, int precision, int block, int k,
     copy_pad_kernel<<<grid_for(n * kb, 256, 4096), 256, 0, s>>>(n, k, kb, evecs, w.Up);
     SG_CHECK_LAUNCH();
     SG_TRY(sg_block_proj(1, kb, n, w.Up, kb, kb, w.Up, w.part32, nparts, w.G32, s));
-    SG_TRY(sg_block_finish(1, kb, n, w.Up, nullptr, 0, 0, nullptr, w.Zs64, op->a, s));
-    SG_TRY(ap.apply(1, kb, rvt, rvx, w.Up, w.Zs64, w.T64, w.W64));
+    if (ds_sweep) {
+      // Zs64 / T64 hold (hi, lo) FP32 pairs here: the same bytes as FP64
+      SG_TRY(sg_ds_split(n, op->a, w.Up, w.Zs64, s));
+      SG_TRY(sg_spmm_ds(0, m, op->colptr, op->rowidx, op->cvalues, w.Zs64, w.T64, op->w2, nullptr, nullptr, rvt,
+                        w.counter, s));
+      SG_TRY(sg_spmm_ds(1, n, op->indptr, op->indices, op->values, w.T64, w.W64, op->a, op->dinv, w.Up, rvx,
+                        w.counter + 1, s));
+      nl += 2;
+    } else {
+      SG_TRY(sg_block_finish(1, kb, n, w.Up, nullptr, 0, 0, nullptr, w.Zs64, op->a, s));
+      SG_TRY(ap.apply(1, kb, rvt, rvx, w.Up, w.Zs64, w.T64, w.W64));
+    }
     SG_TRY(sg_block_proj(1, kb, n, w.Up, kb, kb, w.W64, w.part32, nparts, w.H32, s));
     refine_prep_kernel<<<1, 256, 0, s>>>(k, kb, w.G32, w.H32, w.Ri, w.Cs, w.tmp, status);
     SG_CHECK_LAUNCH();
