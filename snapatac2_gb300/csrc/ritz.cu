@@ -50,13 +50,23 @@ __device__ __forceinline__ double warp_sum_d(double v) {
   return v;
 }
 
-// Shared memory of the reduction: rows [R][n], v[2][n], p[2][n], 2 x 32 slots
-// (per-CTA partial sums of pᵀv in 0..CS-1, τ in 16), 32 per-warp partials.
+// Shared memory of the reduction: rows [R][n], v[2][n], p[2][n], 2 x 32
+// slots (per-CTA partial sums of pᵀv in 0..CS-1, τ in 16), 32 per-warp
+// partials, 4 scalars.  v and the slots are double-buffered: the owner of
+// step j + 1 writes them into the other CTAs before those have finished step
+// j.  p is written by the other CTAs only after the step's first cluster
+// barrier, so the p buffer of the other parity holds w = p + K v.
 inline size_t tridiag_smem(int n, int CS) {
   const int R = (n + CS - 1) / CS;
-  return ((size_t)R * n + 4 * (size_t)n + 64 + 32) * sizeof(double);
+  return ((size_t)R * n + 4 * (size_t)n + 64 + 32 + 4) * sizeof(double);
 }
 
+// GB300 runs FP64 at about two lanes per clock per SM, so a warp-wide FP64
+// instruction holds its SM sub-partition for tens of clocks: the scalar steps
+// (the reflector's norm, square root and divisions, the K factor) run once,
+// on one thread or one warp, and are passed on through shared memory; the
+// vector w = p + K v is formed once per step, and each trailing element is
+// updated by two FMAs.
 template <int CS>
 __global__ void __launch_bounds__(kTriThreads)
 tridiag_kernel(int n, const double* __restrict__ A, int64_t lda, double* __restrict__ d, double* __restrict__ e,
@@ -70,6 +80,7 @@ tridiag_kernel(int n, const double* __restrict__ A, int64_t lda, double* __restr
   double* pb = vb + 2 * n;
   double* slots = pb + 2 * n;
   double* red = slots + 64;
+  double* sc = red + 32;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   for (int t = threadIdx.x; t < R * n; t += blockDim.x) {
     const int li = t / n, c = t % n;
@@ -81,6 +92,7 @@ tridiag_kernel(int n, const double* __restrict__ A, int64_t lda, double* __restr
     const int par = j & 1;
     double* v = vb + par * n;
     double* p = pb + par * n;
+    double* wv = pb + (par ^ 1) * n;
     double* sl = slots + par * 32;
     if (rank == j % CS) {
       // reflector of column j (= row j) below the diagonal, LAPACK dlarfg style
@@ -90,27 +102,42 @@ tridiag_kernel(int n, const double* __restrict__ A, int64_t lda, double* __restr
       s = warp_sum_d(s);
       if (lane == 0) red[warp] = s;
       __syncthreads();
-      double sigma = 0.0;
-      for (int w = 0; w < nwarps; ++w) sigma += red[w];
-      const double alpha = row[j + 1];
-      double tj = 0.0, beta = alpha, scale = 0.0;
-      if (sigma > 0.0) {
-        const double mu = sqrt(fma(alpha, alpha, sigma));
-        beta = alpha <= 0.0 ? mu : -mu;
-        tj = (beta - alpha) / beta;
-        scale = 1.0 / (alpha - beta);
-      }
-      for (int r = 0; r < CS; ++r) {
-        double* rv = CS > 1 ? cl.map_shared_rank(v, r) : v;
-        for (int k = j + 1 + threadIdx.x; k < n; k += blockDim.x) rv[k] = k == j + 1 ? 1.0 : row[k] * scale;
-        if (threadIdx.x == 0) (CS > 1 ? cl.map_shared_rank(sl, r) : sl)[16] = tj;
-      }
-      for (int k = j + 1 + threadIdx.x; k < n; k += blockDim.x)
-        V[(int64_t)j * n + k] = k == j + 1 ? 1.0 : row[k] * scale;
       if (threadIdx.x == 0) {
+        double sigma = 0.0;
+        for (int w = 0; w < nwarps; ++w) sigma += red[w];
+        const double alpha = row[j + 1];
+        double tj = 0.0, beta = alpha, scale = 0.0;
+        if (sigma > 0.0) {
+          const double mu = sqrt(fma(alpha, alpha, sigma));
+          beta = alpha <= 0.0 ? mu : -mu;
+          // τ = (β - α)/β and 1/(α - β) from one reciprocal
+          const double am = alpha - beta;
+          const double inv = 1.0 / (beta * am);
+          tj = -am * am * inv;
+          scale = beta * inv;
+        }
+        sc[0] = tj;
+        sc[1] = scale;
+        sl[16] = tj;
         d[j] = row[j];
         e[j] = beta;
         tau[j] = tj;
+      }
+      __syncthreads();
+      const double scale = sc[1];
+      for (int k = j + 1 + threadIdx.x; k < n; k += blockDim.x) {
+        const double vk = k == j + 1 ? 1.0 : row[k] * scale;
+        v[k] = vk;
+        V[(int64_t)j * n + k] = vk;
+      }
+      __syncthreads();
+      if (CS > 1) {
+        for (int r = 0; r < CS; ++r) {
+          if (r == rank) continue;
+          double* rv = cl.map_shared_rank(v, r);
+          for (int k = j + 1 + threadIdx.x; k < n; k += blockDim.x) rv[k] = v[k];
+          if (threadIdx.x == 0) cl.map_shared_rank(sl, r)[16] = sc[0];
+        }
       }
     }
     if (CS > 1) cl.sync(); else __syncthreads();
@@ -137,19 +164,22 @@ tridiag_kernel(int n, const double* __restrict__ A, int64_t lda, double* __restr
       (CS > 1 ? cl.map_shared_rank(sl, (int)threadIdx.x) : sl)[rank] = s2;
     }
     if (CS > 1) cl.sync(); else __syncthreads();
-    // w = p + K v, K = -τ/2 pᵀv; A <- A - v wᵀ - w vᵀ on the owned trailing rows
-    double K = 0.0;
-    for (int r = 0; r < CS; ++r) K += sl[r];
-    K *= -0.5 * tj;
+    // K = -τ/2 pᵀv (one warp), w = p + K v (once), A <- A - v wᵀ - w vᵀ on
+    // the owned trailing rows
+    if (warp == 0) {
+      const double x = warp_sum_d(lane < CS ? sl[lane] : 0.0);
+      if (lane == 0) sc[3] = -0.5 * tj * x;
+    }
+    __syncthreads();
+    const double K = sc[3];
+    for (int k = j + 1 + threadIdx.x; k < n; k += blockDim.x) wv[k] = fma(K, v[k], p[k]);
+    __syncthreads();
     for (int li = li0 + warp; li < R; li += nwarps) {
       const int i = li * CS + rank;
       if (i >= n) break;
       double* row = Al + (size_t)li * n;
-      const double vi = v[i], wi = fma(K, vi, p[i]);
-      for (int k = j + 1 + lane; k < n; k += 32) {
-        const double wk = fma(K, v[k], p[k]);
-        row[k] -= vi * wk + wi * v[k];
-      }
+      const double vi = v[i], wi = wv[i];
+      for (int k = j + 1 + lane; k < n; k += 32) row[k] = fma(-vi, wv[k], fma(-wi, v[k], row[k]));
     }
     __syncthreads();
   }
@@ -201,42 +231,109 @@ __device__ TriBounds tri_bounds_warp(int n, const double* __restrict__ d, const 
   return b;
 }
 
-// number of eigenvalues of T below x
-__device__ __forceinline__ int sturm_count(int n, const double* __restrict__ d, const double* __restrict__ e,
-                                           double x, double pivmin) {
-  double q = d[0] - x;
-  if (fabs(q) < pivmin) q = -pivmin;
-  int c = q <= 0.0;
+// Number of eigenvalues of T below x (e2 = squared off-diagonal), as the
+// number of sign changes of the Sturm sequence of leading principal minors
+// p_i = (d_i - x) p_{i-1} - e²_{i-1} p_{i-2} (Givens; Wilkinson, The
+// Algebraic Eigenvalue Problem, 5.37-5.45): q_i = p_i / p_{i-1} <= 0 exactly
+// when p_i and p_{i-1} differ in sign.  This form has no division: GB300
+// runs an FP64 division as a chain of dependent FP64 operations (several
+// hundred clocks), so the ratio form q_i = (d_i - x) - e²/q_{i-1} costs about
+// four times as much per step.  The pair (p_i, p_{i-1}) is rescaled by an
+// exact power of two whenever its larger exponent leaves [2^-400, 2^400], so
+// it neither overflows nor underflows.  A zero minor is replaced by a tiny
+// value of the sign opposite to its predecessor, which counts it as
+// negative, as the ratio form's pivot floor does.  Signs and exponents are
+// read as integers, off the FP64 pipe.
+__device__ __forceinline__ int sturm_count(int n, const double* __restrict__ d, const double* __restrict__ e2,
+                                           double x) {
+  constexpr long long kSign = (long long)0x8000000000000000ull;
+  double pm = 1.0;
+  double p = d[0] - x;
+  if (p == 0.0) p = -DBL_MIN;
+  int c = p < 0.0;
   for (int i = 1; i < n; ++i) {
-    q = (d[i] - x) - e[i - 1] * e[i - 1] / q;
-    if (fabs(q) < pivmin) q = -pivmin;
-    c += q <= 0.0;
+    double pn = fma(-e2[i - 1], pm, (d[i] - x) * p);
+    long long bn = __double_as_longlong(pn);
+    const long long bp = __double_as_longlong(p);
+    if ((bn & ~kSign) == 0) {  // zero minor: opposite sign to p, 2^-600 of the pair's scale (a normal number)
+      const double mag = fmax(fabs(p), fabs(pm)) * 0x1p-600;
+      pn = bp < 0 ? mag : -mag;
+      bn = __double_as_longlong(pn);
+    }
+    c += (int)(((unsigned long long)(bn ^ bp)) >> 63);
+    pm = p;
+    p = pn;
+    const int ex = (int)((bn >> 52) & 0x7ff), ey = (int)((bp >> 52) & 0x7ff);
+    const int emax = ex > ey ? ex : ey;
+    if (emax > 1023 + 400 || emax < 1023 - 400) {
+      // multiply both by 2^(1023 - emax), built from its bits
+      const double sc = __longlong_as_double((long long)(2046 - emax) << 52);
+      p *= sc;
+      pm *= sc;
+    }
   }
   return c;
 }
 
-// lam[w] = eigenvalue of ascending rank ranks[w]; one warp per wanted value
-__global__ void bisect_kernel(int n, const double* __restrict__ d, const double* __restrict__ e,
-                              const int* __restrict__ ranks, int nw, double* __restrict__ lam) {
+// lam[w] = eigenvalue of ascending rank ranks[w].  A group of kBisLanes lanes
+// per wanted value evaluates kBisLanes shifts per round (multisection into
+// kBisLanes + 1 parts).  A warp's FP64 instructions run one after another on
+// its sub-partition's FP64 unit whatever the number of active lanes, so the
+// time is rounds x steps x FP64 operations per step of one warp, with one
+// warp per sub-partition (two-warp blocks).  d and e² are staged in shared
+// memory.
+constexpr int kBisLanes = 32;
+constexpr int kBisThreads = 64;
+__global__ void __launch_bounds__(kBisThreads)
+bisect_kernel(int n, const double* __restrict__ d, const double* __restrict__ e, const int* __restrict__ ranks, int nw,
+              double* __restrict__ lam) {
+  __shared__ double ds[kRitzMaxN], e2s[kRitzMaxN];
+  __shared__ TriBounds bs;
+  if (threadIdx.x < 32) {
+    const TriBounds b = tri_bounds_warp(n, d, e);
+    if (threadIdx.x == 0) bs = b;
+  }
+  __syncthreads();
+  // T and the shifts scaled by the power of two that brings ‖T‖ into [0.5, 1):
+  // exact, and it bounds the growth of the minors per step
+  const long long tb = __double_as_longlong(bs.tnorm);
+  const int te = (int)((tb >> 52) & 0x7ff);
+  const double sc = bs.tnorm > 0.0 && te > 0 ? __longlong_as_double((long long)(2045 - te) << 52) : 1.0;
+  const double isc = bs.tnorm > 0.0 && te > 0 ? __longlong_as_double((long long)(te + 1) << 52) : 1.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    ds[i] = d[i] * sc;
+    const double es = i + 1 < n ? e[i] * sc : 0.0;
+    e2s[i] = es * es;
+  }
+  __syncthreads();
   const int lane = threadIdx.x & 31;
-  const int w = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
-  if (w >= nw) return;
-  const TriBounds b = tri_bounds_warp(n, d, e);
-  const int r = ranks[w];
-  double lo = b.lo, hi = b.hi;
+  constexpr int GPW = 32 / kBisLanes;
+  const int g = lane / kBisLanes, gl = lane % kBisLanes;
+  const int w = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5) * GPW + g;
+  if ((int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5) * GPW >= nw) return;  // whole warp idle
+  const bool active = w < nw;
+  const int r = active ? ranks[w] : 0;
+  constexpr double kStep = 1.0 / (kBisLanes + 1);
+  const double tnorm = bs.tnorm * sc;
+  double lo = bs.lo * sc, hi = bs.hi * sc;
+  const unsigned gmask = kBisLanes == 32 ? 0xffffffffu : ((1u << (kBisLanes % 32)) - 1u) << (g * kBisLanes);
   for (int it = 0; it < 64; ++it) {
     const double width = hi - lo;
-    if (width <= fmax(DBL_EPSILON * b.tnorm, 2.0 * DBL_EPSILON * fmax(fabs(lo), fabs(hi))) || width <= 0.0) break;
-    const double x = lo + width * (double)(lane + 1) / 33.0;
-    const int c = sturm_count(n, d, e, x, b.pivmin);
-    const unsigned above = __ballot_sync(0xffffffffu, c > r);
-    const int l = above ? __ffs(above) - 1 : 32;
-    const double nlo = l == 0 ? lo : lo + width * (double)l / 33.0;
-    const double nhi = l == 32 ? hi : lo + width * (double)(l + 1) / 33.0;
-    lo = nlo;
-    hi = nhi;
+    const bool done = !active || width <= 0.0 ||
+                      width <= fmax(DBL_EPSILON * tnorm, 2.0 * DBL_EPSILON * fmax(fabs(lo), fabs(hi)));
+    if (__all_sync(0xffffffffu, done)) break;
+    int c = 0;
+    if (!done) c = sturm_count(n, ds, e2s, lo + width * ((gl + 1) * kStep));
+    const unsigned above = (__ballot_sync(0xffffffffu, c > r) & gmask) >> ((g * kBisLanes) % 32);
+    if (!done) {
+      const int l = above ? __ffs(above) - 1 : kBisLanes;
+      const double nlo = l == 0 ? lo : lo + width * (l * kStep);
+      const double nhi = l == kBisLanes ? hi : lo + width * ((l + 1) * kStep);
+      lo = nlo;
+      hi = nhi;
+    }
   }
-  if (lane == 0) lam[w] = 0.5 * (lo + hi);
+  if (active && gl == 0) lam[w] = 0.5 * (lo + hi) * isc;
 }
 
 __device__ __forceinline__ double hash_unit(uint64_t a, uint64_t b) {
@@ -302,19 +399,26 @@ __global__ void invit_kernel(int n, const double* __restrict__ d, const double* 
       for (int i = 0; i + 1 < n; ++i) {
         const double sub = e[i], dn = d[i + 1] - x, sp = i + 2 < n ? e[i + 1] : 0.0;
         double pv;
+        // one reciprocal per row (an FP64 division is a long chain of FP64
+        // operations here): the multiplier is formed from the pivot's
+        // reciprocal
         if (fabs(cd) >= fabs(sub)) {
-          const double l = cd != 0.0 ? sub / cd : 0.0;
-          pv = cd; U1[i] = cs; U2[i] = 0.0; L[i] = l; P[i] = 0;
+          pv = cd;
+          if (fabs(pv) < tiny) pv = pv < 0.0 ? -tiny : tiny;
+          const double rp = 1.0 / pv;
+          const double l = cd != 0.0 ? sub * rp : 0.0;
+          U0[i] = rp; U1[i] = cs; U2[i] = 0.0; L[i] = l; P[i] = 0;
           cd = dn - l * cs;
           cs = sp;
         } else {
-          const double l = cd / sub;
-          pv = sub; U1[i] = dn; U2[i] = sp; L[i] = l; P[i] = 1;
+          pv = sub;
+          const double rp = 1.0 / pv;
+          const double l = cd * rp;
+          U0[i] = fabs(pv) < tiny ? (pv < 0.0 ? -1.0 / tiny : 1.0 / tiny) : rp;
+          U1[i] = dn; U2[i] = sp; L[i] = l; P[i] = 1;
           cd = cs - l * dn;
           cs = -l * sp;
         }
-        if (fabs(pv) < tiny) pv = pv < 0.0 ? -tiny : tiny;
-        U0[i] = 1.0 / pv;
       }
       if (fabs(cd) < tiny) cd = cd < 0.0 ? -tiny : tiny;
       U0[n - 1] = 1.0 / cd;
@@ -572,7 +676,8 @@ int ritz_values(int n, const double* A, int64_t lda, int p, int q, const RitzLay
   if (err) return err;
   ranks_kernel<<<grid_for(cnt, 256), 256, 0, s>>>(n, p, q, L.ranks);
   SG_CHECK_LAUNCH();
-  bisect_kernel<<<grid_for((int64_t)cnt * 32, 128), 128, 0, s>>>(n, L.d, L.e, L.ranks, cnt, L.lam);
+  bisect_kernel<<<grid_for((int64_t)cnt * kBisLanes, kBisThreads), kBisThreads, 0, s>>>(n, L.d, L.e, L.ranks, cnt,
+                                                                                         L.lam);
   SG_CHECK_LAUNCH();
   return SG_OK;
 }
