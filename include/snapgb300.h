@@ -484,7 +484,8 @@ typedef struct sg_gram_op {
 typedef struct sg_lanczos_opts {
   int basis;                /* Krylov basis size M (multiple of block)       */
   int keep;                 /* thick-restart size                            */
-  double tol_vec;           /* residual bar (x max|θ|) of returned vectors   */
+  double tol_vec;           /* residual bar (x max|θ|) of returned vectors,  */
+                            /* default 3e-9                                  */
   double tol_val;           /* residual bar of the other wanted pairs        */
   int vec_positive_only;    /* 1: vectors returned for θ > 0 only (as        */
                             /* weighted_by_sd keeps), others need tol_val    */

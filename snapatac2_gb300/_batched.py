@@ -132,7 +132,7 @@ class BatchedResult:
 
 
 def eigsh_lm_batched(bop: BatchedOperator, k: int, *, precision: str = "mixed", block: int = 8,
-                     max_basis: int | None = None, keep: int | None = None, tol_vec: float = 1e-8,
+                     max_basis: int | None = None, keep: int | None = None, tol_vec: float = _eigen.TOL_VEC,
                      tol_val: float = 1e-6, seed: int = 0, max_restarts: int = 200, use_graphs: bool = True,
                      threads: int = 16, refine: bool = True) -> BatchedResult:
     L = _lib.lib()

@@ -144,6 +144,11 @@ class GramOperator:
 # Largest Ritz problem (basis + block) the GPU Rayleigh-Ritz holds on one
 # thread-block cluster.
 RITZ_MAX = 640
+# Residual bar (x max|θ|) of the returned vectors: the loosest that kept every
+# returned vector within 1e-4 rad of a solution converged to 1e-12 at 100,000
+# cells, including the dense cluster of small eigenvalues cut by the k-th /
+# (k+1)-th boundary (1e-8 left it at 1.6e-4 rad with block 16; 3e-9: 3e-5).
+TOL_VEC = 3e-9
 
 # Residual level (relative to |A|) below which a stalled mixed-precision
 # solve is taken to sit at its FP32 noise floor (~ 2^-24 times a few hundred).
@@ -397,7 +402,7 @@ def _spmm_choice(op: GramOperator, code: int, block: int, stream: int, staged: b
 
 def eigsh_lm(op: GramOperator, k: int, *, precision: str = "mixed", block: int | None = 8,
              max_basis: int | None = None,
-             keep: int | None = None, tol_vec: float = 1e-8, tol_val: float = 1e-6, vec_positive_only: bool = True,
+             keep: int | None = None, tol_vec: float = TOL_VEC, tol_val: float = 1e-6, vec_positive_only: bool = True,
              seed: int = 0, max_restarts: int = 200, stream: torch.cuda.Stream | None = None,
              refine: bool = True) -> EigenResult:
     """k eigenpairs of largest magnitude (ARPACK ``which='LM'``) of ``op``,
@@ -504,10 +509,10 @@ def _default_basis(k: int, block: int, n: int) -> tuple[int, int]:
 
 
 # Vector matvecs a solve needs at each block size, relative to block 8 (k =
-# 30, tol 1e-8): 100,000 cells 0.68 / 1 / 1.32 / 1.96 and 1,000,000 cells
-# - / 1 / 1.46 / 2.40 for blocks 4 / 8 / 16 / 32.  The prior of the block
+# 30, tol_vec 3e-9): 100,000 cells 0.75 / 1 / 1.47 / 2.27 and 1,000,000 cells
+# - / 1 / 1.52 / - for blocks 4 / 8 / 16 / 32.  The prior of the block
 # choice; observed solves of the same shape class replace it.
-BLOCK_PRIOR = {4: 0.68, 8: 1.0, 16: 1.39, 32: 2.18}
+BLOCK_PRIOR = {4: 0.75, 8: 1.0, 16: 1.49, 32: 2.27}
 _BLOCK_CHOICE: dict = {}   # shape class -> (block, predicted seconds per block)
 _BLOCK_SEEN: dict = {}     # shape class -> {block: vector matvecs of the last solve}
 _RITZ_MS: dict = {}        # basis size -> measured ms of one GPU Rayleigh-Ritz step
@@ -659,7 +664,7 @@ def choose_block(op: GramOperator, k: int, precision: str = "mixed", stream: int
 
 
 def eigsh_lm_host_ritz(op: GramOperator, k: int, *, precision: str = "mixed", block: int = 8,
-                       max_basis: int | None = None, keep: int | None = None, tol_vec: float = 1e-8,
+                       max_basis: int | None = None, keep: int | None = None, tol_vec: float = TOL_VEC,
                        tol_val: float = 1e-6, vec_positive_only: bool = True, seed: int = 0, max_restarts: int = 200,
                        stream: torch.cuda.Stream | None = None, refine: bool = True) -> EigenResult:
     """The same solver driven step by step from Python with the Ritz problem

@@ -208,27 +208,35 @@ __global__ void refine_prep_kernel(int k, int kb, const double* __restrict__ G, 
   }
 }
 
-// Y = Ri Z (Z rows = eigenvectors of C, ascending), columns in descending
-// eigenvalue order; evals out descending.
-__global__ void refine_finish_kernel(int k, const double* __restrict__ Ri, const double* __restrict__ lam,
+// Of the kr refined pairs (lam ascending, Z rows = eigenvectors of C) the k
+// of largest |λ| (ties: the smaller value first, as numpy's stable argsort of
+// -|θ| over eigh's ascending output), in descending eigenvalue order:
+// Y = Ri Z[:, chosen] (kr x k), evals descending.  One CTA.
+__global__ void refine_finish_kernel(int k, int kr, const double* __restrict__ Ri, const double* __restrict__ lam,
                                      const double* __restrict__ Zt, double* __restrict__ Y,
                                      double* __restrict__ evals) {
-  for (int t = threadIdx.x; t < k * k; t += blockDim.x) {
-    const int p = t / k, c = t % k;  // row p of Y, output column c = eigenpair k-1-c
-    const double* z = Zt + (size_t)(k - 1 - c) * k;
+  __shared__ int pick[32];
+  if (threadIdx.x == 0) {
+    int c = 0;
+    for (int i = kr - 1; i >= 0; --i) {  // descending value
+      const double ai = fabs(lam[i]);
+      int pos = 0;
+      for (int o = 0; o < kr; ++o) {
+        const double ao = fabs(lam[o]);
+        pos += (ao > ai) || (ao == ai && o < i);
+      }
+      if (pos < k) pick[c++] = i;
+    }
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < kr * k; t += blockDim.x) {
+    const int p = t / k, c = t % k;
+    const double* z = Zt + (size_t)pick[c] * kr;
     double s = 0.0;
-    for (int q = 0; q < k; ++q) s = fma(Ri[p * k + q], z[q], s);
+    for (int q = 0; q < kr; ++q) s = fma(Ri[p * kr + q], z[q], s);
     Y[t] = s;
   }
-  for (int c = threadIdx.x; c < k; c += blockDim.x) evals[c] = lam[k - 1 - c];
-}
-
-__global__ void copy_pad_kernel(int64_t n, int k, int kb, const double* __restrict__ U, double* __restrict__ Up) {
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n * kb; t += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t i = t / kb;
-    const int c = (int)(t % kb);
-    Up[t] = c < k ? U[i * k + c] : 0.0;
-  }
+  for (int c = threadIdx.x; c < k; c += blockDim.x) evals[c] = lam[pick[c]];
 }
 
 // ---------------------------------------------------------------------------
@@ -428,7 +436,12 @@ extern "C" int sg_lanczos(const sg_gram_op* op, int precision, int block, int k,
     o.max_restarts = -1;
     o.variant_t = o.variant_x = o.refine_variant_t = o.refine_variant_x = -1;
   }
-  const double tol_vec = o.tol_vec > 0 ? o.tol_vec : 1e-8;
+  // 3e-9: at 100,000 cells x 500,000 features the wanted eigenvalues end in a
+  // dense cluster of small ones (relative gaps ~2e-4) that the k-th / (k+1)-th
+  // boundary cuts; with 1e-8 the returned vectors of that cluster stayed up to
+  // 1.6e-4 rad from a solution converged to 1e-12 (block 16), with 3e-9
+  // within 3e-5 rad (block 8: 5.3e-5)
+  const double tol_vec = o.tol_vec > 0 ? o.tol_vec : 3e-9;
   const double tol_val = o.tol_val > 0 ? o.tol_val : 1e-6;
   const int max_restarts = o.max_restarts >= 0 ? o.max_restarts : 200;
   const int vt = o.variant_t >= 0 ? o.variant_t : default_variant(code, 0);
@@ -549,18 +562,21 @@ extern "C" int sg_lanczos(const sg_gram_op* op, int precision, int block, int k,
     ph_restart += now_s() - tq;
   }
   const double tf = now_s();
-  // Ritz vectors (FP64 output), eigenvalues descending like the reference
-  SG_TRY(sg_basis_rotate(code, 1, n, Q, ld, Me, w.Yf, k, k, evecs, k, s));
-  ++nl;
   double* ev_dev = w.evals_f;
   const int64_t solve_spmm = ap.spmm_launches;
   ap.timed = false;  // the event times cover the solve's own SpMM launches
   if (o.refine && code == 0 && k <= 32) {
-    // FP64 correction sweep: U padded to 32 columns, G = UᵀU, Hm = Uᵀ A U in
-    // FP64, generalized eigenproblem Hm y = θ G y by Cholesky, U <- U Y
+    // Correction sweep over the k wanted Ritz vectors and the next ones in
+    // |θ| order up to 32 (guard vectors): U = Q Yk[:, :kr], G = UᵀU and
+    // Hm = Uᵀ A U in FP64-class arithmetic, generalized eigenproblem
+    // Hm y = θ G y by Cholesky, the k of largest |θ| returned.  The guards
+    // let the sweep separate a wanted pair from an unwanted one close to it
+    // (the k-th and (k+1)-th eigenvalues of a tight cluster), which a sweep
+    // over the k vectors alone cannot.
     const int kb = 32;
-    copy_pad_kernel<<<grid_for(n * kb, 256, 4096), 256, 0, s>>>(n, k, kb, evecs, w.Up);
-    SG_CHECK_LAUNCH();
+    const int kr = std::min(kb, keep);
+    if (kr < kb && cudaMemsetAsync(w.Up, 0, sizeof(double) * n * kb, s) != cudaSuccess) return SG_ERR_CUDA;
+    SG_TRY(sg_basis_rotate(code, 1, n, Q, ld, Me, w.Yk, keep, kr, w.Up, kb, s));
     SG_TRY(sg_block_proj(1, kb, n, w.Up, kb, kb, w.Up, w.part32, nparts, w.G32, s));
     if (ds_sweep) {
       // Zs64 / T64 hold (hi, lo) FP32 pairs here: the same bytes as FP64
@@ -569,24 +585,29 @@ extern "C" int sg_lanczos(const sg_gram_op* op, int precision, int block, int k,
                         w.counter, s));
       SG_TRY(sg_spmm_ds(1, n, op->indptr, op->indices, op->values, w.T64, w.W64, op->a, op->dinv, w.Up, rvx,
                         w.counter + 1, s));
-      nl += 2;
+      nl += 3;
     } else {
       SG_TRY(sg_block_finish(1, kb, n, w.Up, nullptr, 0, 0, nullptr, w.Zs64, op->a, s));
       SG_TRY(ap.apply(1, kb, rvt, rvx, w.Up, w.Zs64, w.T64, w.W64));
+      ++nl;
     }
     SG_TRY(sg_block_proj(1, kb, n, w.Up, kb, kb, w.W64, w.part32, nparts, w.H32, s));
-    refine_prep_kernel<<<1, 256, 0, s>>>(k, kb, w.G32, w.H32, w.Ri, w.Cs, w.tmp, status);
+    refine_prep_kernel<<<1, 256, 0, s>>>(kr, kb, w.G32, w.H32, w.Ri, w.Cs, w.tmp, status);
     SG_CHECK_LAUNCH();
-    nl += 3 + 2 * proj_launches(1, kb, kb) + 1;
+    nl += 2 + 2 * proj_launches(1, kb, kb);
     int nw2 = 0;
-    SG_TRY(ritz_values(k, w.Cs, k, k, 0, w.ritz32, &nw2, s));
-    SG_TRY(ritz_vectors(k, w.ritz32, nullptr, nw2, s));
+    SG_TRY(ritz_values(kr, w.Cs, kr, kr, kr, w.ritz32, &nw2, s));
+    SG_TRY(ritz_vectors(kr, w.ritz32, nullptr, nw2, s));
     nl += 7;
-    refine_finish_kernel<<<1, 256, 0, s>>>(k, w.Ri, w.ritz32.lam, w.ritz32.Zt, w.Yr, w.ev32);
+    refine_finish_kernel<<<1, 256, 0, s>>>(k, kr, w.Ri, w.ritz32.lam, w.ritz32.Zt, w.Yr, w.ev32);
     SG_CHECK_LAUNCH();
-    SG_TRY(sg_basis_rotate(1, 1, n, w.Up, kb, k, w.Yr, k, k, evecs, k, s));
+    SG_TRY(sg_basis_rotate(1, 1, n, w.Up, kb, kr, w.Yr, k, k, evecs, k, s));
     nl += 2;
     ev_dev = w.ev32;
+  } else {
+    // Ritz vectors (FP64 output), eigenvalues descending like the reference
+    SG_TRY(sg_basis_rotate(code, 1, n, Q, ld, Me, w.Yf, k, k, evecs, k, s));
+    ++nl;
   }
   std::vector<double> res_h(k);
   int st = 0;
