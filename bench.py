@@ -430,7 +430,8 @@ def large_stage(args, dev):
     r = _eigen.residual_norms(op, res.evecs, res.evals)
     anorm = float(np.max(np.abs(res.evals)))
     t = time.perf_counter()
-    res64 = _eigen.eigsh_lm(op, args.ncomps, precision="fp64", block=8)
+    res64 = _eigen.eigsh_lm(op, args.ncomps, precision="fp64", block=8, tol_vec=1e-10, tol_val=1e-10,
+                            vec_positive_only=False)  # reference converged past the mixed form's bar
     torch.cuda.synchronize(dev)
     t64 = time.perf_counter() - t
     acc = accuracy_block(res.evals, res.evecs.cpu().numpy(), res64.evals, res64.evecs.cpu().numpy(),
@@ -440,8 +441,8 @@ def large_stage(args, dev):
                         f"spectral n_comps={args.ncomps} (mixed) + exact kNN k=50; CSR resident in HBM",
             "target_wall_s": 30, "autotuned_block": auto,
             "block_choice_predicted_ms": _block_prediction(n, m, csr.nnz, args.ncomps), **runs,
-            "accuracy_vs_fp64_gpu": {**acc, "compared_block": b, "fp64_form_s": t64,
-                                     "fp64_block_matvecs": res64.info["block_matvecs"]},
+            "accuracy_vs_fp64_gpu": {**acc, "compared_block": b, "fp64_reference_tol": 1e-10,
+                                     "fp64_reference_s": t64, "fp64_block_matvecs": res64.info["block_matvecs"]},
             "max_residual_rel": float(np.max(r) / anorm),
             "residual_note": "FP64 ||A u - λ u|| / max|λ| of the returned mixed-precision eigenpairs",
             "knn_checked_rows": checked, "knn_sample_identical_to_oracle": same, "clocks": clk}
@@ -700,6 +701,13 @@ def run_gpu(args):
                             "reported separately",
                     "lm_set_magnitude_rel_err_max": float(np.max(np.abs(np.sort(np.abs(ev)) - np.sort(np.abs(ev64)))
                                                                  / np.sort(np.abs(ev64))))}
+        # the same comparison against an all-FP64 solve converged to 1e-11 (untimed): the
+        # open-boundary cluster's angle then measures the mixed result, not both
+        ev_t, U_t, info_t = spectral_embedding(csr, None, args.ncomps, 0, precision="fp64", block=8, tol_vec=1e-11,
+                                               tol_val=1e-11, vec_positive_only=False, return_info=True)
+        tight = accuracy_block(np.asarray(ev), U.cpu().numpy(), np.asarray(ev_t), U_t.cpu().numpy(),
+                               info_t.get("next_evals", [None])[0])
+        accuracy["vs_fp64_converged_1e-11"] = {**tight, "fp64_block_matvecs": info_t["block_matvecs"]}
 
     # ---- gather floor of the SpMM passes (diagnostic, after the timed legs) --
     gather = gather_ceiling(csr, infos[-1]["block"], dev) if rank == 0 else None
