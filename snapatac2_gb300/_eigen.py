@@ -499,20 +499,22 @@ class EigenResult:
 
 
 def _default_basis(k: int, block: int, n: int) -> tuple[int, int]:
-    """Basis size M and thick-restart size: keep ≈ 2.7 k, M ≈ keep + 15 blocks
-    (k = 30, b = 8: keep 80, M 200; measured on 100k-cell data to cut block
-    matvecs by a third against keep 46 / M 144 at the same accuracy)."""
-    keep = max(k + 2 * block, int(round(2.67 * k)))
-    M = keep + max(15 * block, 96)
+    """Basis size M and thick-restart size, as the library's default:
+    keep ≈ 3.2 k, M ≈ keep + max(18 blocks, 7.5 k), at most the Rayleigh-Ritz
+    limit (k = 30: keep 96, M 384 at block 16; measured at 100k cells to need
+    6 restarts and 132 block matvecs against 8 and 140 with keep 80 / M 320)."""
+    keep = max(k + 2 * block, int(round(3.2 * k)))
+    M = keep + max(18 * block, int(round(7.5 * k)))
     M = int(math.ceil(M / block) * block)
+    M = min(M, (RITZ_MAX - block) // block * block)
     return M, keep
 
 
 # Vector matvecs a solve needs at each block size, relative to block 8 (k =
-# 30, tol_vec 3e-9): 100,000 cells 0.75 / 1 / 1.47 / 2.27 and 1,000,000 cells
-# - / 1 / 1.52 / - for blocks 4 / 8 / 16 / 32.  The prior of the block
-# choice; observed solves of the same shape class replace it.
-BLOCK_PRIOR = {4: 0.75, 8: 1.0, 16: 1.49, 32: 2.27}
+# 30, tol_vec 3e-9, default basis): 100,000 cells 0.83 / 1 / 1.42 / 2.13 and
+# 1,000,000 cells - / 1 / 1.45 / - for blocks 4 / 8 / 16 / 32.  The prior of
+# the block choice; observed solves of the same shape class replace it.
+BLOCK_PRIOR = {4: 0.83, 8: 1.0, 16: 1.43, 32: 2.13}
 _BLOCK_CHOICE: dict = {}   # shape class -> (block, predicted seconds per block)
 _BLOCK_SEEN: dict = {}     # shape class -> {block: vector matvecs of the last solve}
 _RITZ_MS: dict = {}        # basis size -> measured ms of one GPU Rayleigh-Ritz step

@@ -177,7 +177,10 @@ def spectral_nystrom(X, features=None, n_comps: int = 30, sample_size: int = 100
         if precision == "auto":
             from .tools import AUTO_FP64_CELLS
             precision = "fp64" if op_s.n < AUTO_FP64_CELLS else "mixed"
-        res = _eigen.eigsh_lm(op_s, n_comps, precision=precision, block=block, seed=random_state)
+        # every landmark eigenvector enters the extension and the orthogonalisation
+        # (negative ones included), so all are converged to the vector bar
+        res = _eigen.eigsh_lm(op_s, n_comps, precision=precision, block=block, seed=random_state,
+                              vec_positive_only=False)
         v = np.asarray(res.evals, dtype=np.float64)
         k = v.size
         sh = torch.cuda.current_stream(dev).cuda_stream
