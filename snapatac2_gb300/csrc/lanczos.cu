@@ -493,9 +493,13 @@ bool tiled_ok(const void* Q, int64_t ldq, const void* W) {
 // memory (no per-thread local arrays).
 __global__ void chol_kernel(int B, const double* __restrict__ G, double* __restrict__ R,
                             double* __restrict__ Rinv, int* status) {
+  // FP64 divisions and square roots are long dependent chains on GB300's
+  // FP64 unit: each pivot takes one reciprocal square root (r_kk = s·rsqrt(s),
+  // 1/r_kk = rsqrt(s)) and every division becomes a product with it
   __shared__ double g[32][33];
   __shared__ double r[32][33];
   __shared__ double x[32][33];  // x[i][j]: row i of column j of R⁻¹
+  __shared__ double rd[32];     // 1 / r[k][k]
   const int j = threadIdx.x;
   for (int t = j; t < B * B; t += 32) g[t / B][t % B] = G[t];
   for (int i = 0; i < B; ++i) {
@@ -510,29 +514,68 @@ __global__ void chol_kernel(int B, const double* __restrict__ G, double* __restr
       for (int i = 0; i < k; ++i) s -= r[i][k] * r[i][k];
       const double gkk = g[k][k];
       if (!(s > 1e-28 * (gkk > 0 ? gkk : 1.0)) || !(s > 0.0)) { fail = true; s = 1.0; }
-      r[k][k] = sqrt(s);
+      const double rs = rsqrt(s);
+      r[k][k] = s * rs;
+      rd[k] = rs;
     }
     __syncwarp();
-    const double piv = r[k][k];
+    const double ip = rd[k];
     if (j > k && j < B) {
       double s = g[k][j];
       for (int i = 0; i < k; ++i) s -= r[i][k] * r[i][j];
-      r[k][j] = s / piv;
+      r[k][j] = s * ip;
     }
     __syncwarp();
   }
   if (__any_sync(0xffffffffu, fail) && j == 0) atomicCAS(status, 0, SG_ERR_NUMERIC);
   // back substitution, lane j computes column j of R^-1
   if (j < B) {
-    x[j][j] = 1.0 / r[j][j];
+    x[j][j] = rd[j];
     for (int i = j - 1; i >= 0; --i) {
       double s = 0.0;
       for (int t = i + 1; t <= j; ++t) s += r[i][t] * x[t][j];
-      x[i][j] = -s / r[i][i];
+      x[i][j] = -s * rd[i];
     }
     for (int i = 0; i < B; ++i) {
       Rinv[i * B + j] = i <= j ? x[i][j] : 0.0;
       R[i * B + j] = r[i][j];
+    }
+  }
+}
+
+// W[i,:] <- W[i,:] Rinv, FP32 blocks of 16: thread per row, the row in
+// registers, Rinv in shared memory read as broadcasts; column c sums
+// W[i,k] Rinv[k,c] over k = 0..c in order (the order of the warp form)
+template <int B>
+__global__ void __launch_bounds__(256) apply_rinv_rows(int64_t n, const double* __restrict__ Rinv,
+                                                      float* __restrict__ W) {
+  __shared__ float ri[B][B];
+  for (int t = threadIdx.x; t < B * B; t += blockDim.x) ri[t / B][t % B] = (float)Rinv[t];
+  __syncthreads();
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    float w[B];
+    const float4* wr = reinterpret_cast<const float4*>(W + i * B);
+#pragma unroll
+    for (int q = 0; q < B / 4; ++q) {
+      const float4 v = wr[q];
+      w[4 * q] = v.x;
+      w[4 * q + 1] = v.y;
+      w[4 * q + 2] = v.z;
+      w[4 * q + 3] = v.w;
+    }
+    float4* wo = reinterpret_cast<float4*>(W + i * B);
+#pragma unroll
+    for (int q = 0; q < B / 4; ++q) {  // four output columns at a time
+      float o[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int c = 4 * q + u;
+        float s = 0.f;
+#pragma unroll
+        for (int k = 0; k <= c; ++k) s = fmaf(w[k], ri[k][c], s);
+        o[u] = s;
+      }
+      wo[q] = make_float4(o[0], o[1], o[2], o[3]);
     }
   }
 }
@@ -785,10 +828,14 @@ template <typename T>
 int rinv_dispatch(int B, int64_t n, const double* Rinv, T* W, cudaStream_t s) {
   const int grid = grid_for(n, 256, 16 * sm_count_l());
   const int gridw = grid_for(n * 32, 256, 8 * sm_count_l());
+  const bool rows_ok = sizeof(T) == 4 && ((uintptr_t)W & 15u) == 0;
   switch (B) {
     case 4: apply_rinv<T, 4><<<grid, 256, 0, s>>>(n, Rinv, W); break;
     case 8: apply_rinv<T, 8><<<grid, 256, 0, s>>>(n, Rinv, W); break;
-    case 16: apply_rinv_warp<T, 16><<<gridw, 256, 0, s>>>(n, Rinv, W); break;
+    case 16:
+      if (rows_ok) apply_rinv_rows<16><<<grid, 256, 0, s>>>(n, Rinv, reinterpret_cast<float*>(W));
+      else apply_rinv_warp<T, 16><<<gridw, 256, 0, s>>>(n, Rinv, W);
+      break;
     case 32: apply_rinv_warp<T, 32><<<gridw, 256, 0, s>>>(n, Rinv, W); break;
     default: return SG_ERR_ARG;
   }
