@@ -451,11 +451,11 @@ extern "C" int sg_lanczos(const sg_gram_op* op, int precision, int block, int k,
   const int max_restarts = o.max_restarts >= 0 ? o.max_restarts : 200;
   const int vt = o.variant_t >= 0 ? o.variant_t : default_variant(code, 0);
   const int vx = o.variant_x >= 0 ? o.variant_x : default_variant(code, 1);
-  // correction sweep: refine 1 = compensated FP32 kernels (variants of sg_spmm_ds; dynamic rows and
-  // two index chunks for the skewed feature rows, static for the cells), 2 = FP64 kernels
+  // correction sweep: refine 1 = compensated FP32 kernels (variants of sg_spmm_ds: dynamic rows and
+  // two index chunks in flight, the fastest for both passes at 100k and 1M cells), 2 = FP64 kernels
   const bool ds_sweep = o.refine != 2;
   const int rvt = o.refine_variant_t >= 0 ? o.refine_variant_t : (ds_sweep ? 3 : default_variant(1, 0));
-  const int rvx = o.refine_variant_x >= 0 ? o.refine_variant_x : (ds_sweep ? 1 : default_variant(1, 1));
+  const int rvx = o.refine_variant_x >= 0 ? o.refine_variant_x : (ds_sweep ? 3 : default_variant(1, 1));
   if (ds_sweep && (rvt > 3 || rvx > 3)) return SG_ERR_ARG;
   Basis bs = default_basis(k, b);
   int M = o.basis > 0 ? o.basis : bs.M;
