@@ -356,6 +356,22 @@ int sg_csr_row_norms(int64_t n, const int64_t* indptr, const int32_t* indices, c
 int sg_spmm_dyn(int dtype, int block, int64_t rows, const int64_t* ptr, const int32_t* idx, const float* val,
                 const void* in, void* out, const void* scale, const void* dshift, const void* y, int variant,
                 const unsigned char* row_mask, unsigned int* counter, void* stream);
+/* sg_spmm_dyn over a row order: the counter walks `positions` positions and */
+/* order[p] (device int32, -1 = none) is the row at position p.  With the   */
+/* order of sg_row_order the longest rows are taken first, one per 4-row     */
+/* fetch, so the last rows to finish are short (longest-first scheduling of */
+/* the Xᵀ pass, whose rows are features of very different lengths).  Same   */
+/* per-row arithmetic and result as sg_spmm_dyn.  No reference counterpart. */
+int sg_spmm_dyn_ordered(int dtype, int block, int64_t positions, const int64_t* ptr, const int32_t* idx,
+                        const float* val, const void* in, void* out, const void* scale, const void* dshift,
+                        const void* y, int variant, const int32_t* order, unsigned int* counter, void* stream);
+/* Row order of a CSR by descending row length (ties: ascending row), dealt */
+/* so that position 4c + j holds the row of rank c + j * ceil(rows / 4):    */
+/* order has sg_row_order_positions(rows) entries; scratch of               */
+/* sg_row_order_scratch_bytes(rows) bytes, 256-byte aligned.                */
+int64_t sg_row_order_positions(int64_t rows);
+int64_t sg_row_order_scratch_bytes(int64_t rows);
+int sg_row_order(int64_t rows, const int64_t* ptr, int32_t* order, void* scratch, int64_t scratch_bytes, void* stream);
 
 /* Stage-tiled SpMM, same result contract as sg_spmm_masked (summation     */
 /* order differs at rounding level).  One CTA per SM (and wave) owns a row  */
@@ -388,12 +404,14 @@ int sg_spmm_staged(int dtype, int block, int64_t rows, int64_t cols, const int64
 /* M is the CSR (ptr, idx, val; val NULL: all ones).  in, out, y 16-byte    */
 /* aligned; out must not alias in.  Variants 0-3: one or two 32-index       */
 /* chunks in flight (bit 0), static or counter-driven row schedule (bit 1,  */
-/* needs `counter`, zeroed by the call).  Deterministic.  No reference      */
+/* needs `counter`, zeroed by the call).  `order` (counter-driven variants  */
+/* only, else NULL): a row order as for sg_spmm_dyn_ordered, `rows` then    */
+/* being its number of positions.  Deterministic.  No reference             */
 /* counterpart (an arithmetic form of the FP64 matvec).                     */
 int sg_spmm_ds_variants(void);
 int sg_spmm_ds(int pass, int64_t rows, const int64_t* ptr, const int32_t* idx, const float* val, const void* in,
                void* out, const double* scale, const double* dshift, const double* y, int variant,
-               unsigned int* counter, void* stream);
+               const int32_t* order, unsigned int* counter, void* stream);
 /* out[r, c] = (hi, lo) pair of a[r] * U[r, c] (a NULL: of U[r, c]); U is   */
 /* n x 32 FP64, out n x 32 pairs of FP32 (hi = fl32(v), lo = fl32(v - hi)). */
 int sg_ds_split(int64_t n, const double* a, const double* U, void* out, void* stream);
@@ -477,6 +495,10 @@ typedef struct sg_gram_op {
   const float* dinv_f32;
   const void* staged_table_t;                   /* stage-tiled SpMM segment   */
   const void* staged_table_x;                   /* tables, or NULL            */
+  const int32_t* order_t;                       /* sg_row_order of the CSC    */
+  int64_t order_t_positions;                    /* (longest columns first for */
+                                                /* the dynamic Xᵀ pass), or   */
+                                                /* NULL / 0                   */
 } sg_gram_op;
 
 /* Solver settings; zero / negative fields take the defaults (a NULL opts   */

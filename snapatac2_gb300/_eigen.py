@@ -67,6 +67,22 @@ class GramOperator:
     status: object = None  # DeviceStatus of the staged SpMM's bounded waits (created on first use)
     staged_tables: dict = field(default_factory=dict)  # (pass, row bytes) -> segment table (uint8)
     counter: torch.Tensor | None = None  # row counters of the dynamically scheduled SpMM (one per pass)
+    order_t: torch.Tensor | None = None  # int32 positions -> CSC rows, longest first (sg_row_order)
+
+    def row_order_t(self, stream: int) -> torch.Tensor:
+        """The CSC's rows (features) by descending length, dealt one per
+        4-row fetch (``sg_row_order``): the order in which the dynamically
+        scheduled Xᵀ pass takes them.  Built once per operator."""
+        if self.order_t is None:
+            L = _lib.load()
+            npos = int(L.sg_row_order_positions(self.m))
+            order = torch.empty(max(npos, 1), dtype=torch.int32, device=self.a.device)
+            nb = int(L.sg_row_order_scratch_bytes(self.m))
+            scratch = torch.empty(nb, dtype=torch.uint8, device=self.a.device)
+            _lib.check(L.sg_row_order(self.m, self.colptr.data_ptr(), order.data_ptr(), scratch.data_ptr(), nb,
+                                      stream), "sg_row_order")
+            self.order_t = order[:npos]
+        return self.order_t
 
     def scales(self, dtype_code: int):
         if dtype_code == 0:
@@ -103,9 +119,15 @@ class GramOperator:
         if variant >= DYN:
             if self.counter is None:
                 self.counter = torch.zeros(2, dtype=torch.int32, device=self.a.device)
-            rc = L.sg_spmm_dyn(dtype_code, block, rows, ptr.data_ptr(), idx.data_ptr(), val, inp.data_ptr(),
-                               out.data_ptr(), scale, dsh, yp, variant - DYN, mask,
-                               self.counter.data_ptr() + 4 * which, stream)
+            if which == 0 and mask is None and self.m > 0:  # longest features first
+                order = self.row_order_t(stream)
+                rc = L.sg_spmm_dyn_ordered(dtype_code, block, order.numel(), ptr.data_ptr(), idx.data_ptr(), val,
+                                           inp.data_ptr(), out.data_ptr(), scale, dsh, yp, variant - DYN,
+                                           order.data_ptr(), self.counter.data_ptr(), stream)
+            else:
+                rc = L.sg_spmm_dyn(dtype_code, block, rows, ptr.data_ptr(), idx.data_ptr(), val, inp.data_ptr(),
+                                   out.data_ptr(), scale, dsh, yp, variant - DYN, mask,
+                                   self.counter.data_ptr() + 4 * which, stream)
         elif variant >= STAGED:
             if self.status is None:
                 self.status = _lib.DeviceStatus(self.a.device)
@@ -456,9 +478,10 @@ def eigsh_lm(op: GramOperator, k: int, *, precision: str = "mixed", block: int |
     tab_x = tt.get((1, block * (4 if code == 0 else 8)))
     csr = op.csr
     p = lambda t: t.data_ptr() if t is not None else None  # noqa: E731
+    order_t = op.row_order_t(sh) if op.m > 0 else None
     gop = _lib.GramOp(n, op.m, p(csr.indptr), p(csr.indices), p(csr.data), p(op.colptr), p(op.rowidx),
                       p(op.cvalues), p(op.w2), p(op.a), p(op.dinv), p(op.w2_32), p(op.a32), p(op.dinv32),
-                      p(tab_t), p(tab_x))
+                      p(tab_t), p(tab_x), p(order_t), order_t.numel() if order_t is not None else 0)
     opts = _lib.LanczosOpts(M, keep, float(tol_vec), float(tol_val), int(bool(vec_positive_only)), int(max_restarts),
                             int(do_refine), vt, vx, rvt, rvx, int(SPMM_EVENTS is not None))
     info = _lib.LanczosInfo()

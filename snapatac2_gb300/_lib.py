@@ -90,7 +90,11 @@ SIGNATURES: dict[str, tuple] = {
     "sg_spmm_staged_variants": (_I32, []),
     "sg_spmm_dyn": (_I32, [_I32, _I32, _I64, _P, _P, _P, _P, _P, _P, _P, _P, _I32, _P, _P, _P]),
     "sg_spmm_ds_variants": (_I32, []),
-    "sg_spmm_ds": (_I32, [_I32, _I64, _P, _P, _P, _P, _P, _P, _P, _P, _I32, _P, _P]),
+    "sg_spmm_ds": (_I32, [_I32, _I64, _P, _P, _P, _P, _P, _P, _P, _P, _I32, _P, _P, _P]),
+    "sg_spmm_dyn_ordered": (_I32, [_I32, _I32, _I64, _P, _P, _P, _P, _P, _P, _P, _P, _I32, _P, _P, _P]),
+    "sg_row_order_positions": (_I64, [_I64]),
+    "sg_row_order_scratch_bytes": (_I64, [_I64]),
+    "sg_row_order": (_I32, [_I64, _P, _P, _P, _I64, _P]),
     "sg_ds_split": (_I32, [_I64, _P, _P, _P, _P]),
     "sg_idf_from_counts": (_I32, [_I64, _I64, _P, _P, _P, _P]),
     "sg_csr_row_norms": (_I32, [_I64, _P, _P, _P, _P, _P, _P, _P, _P]),
@@ -126,7 +130,8 @@ class GramOp(ctypes.Structure):
     """``sg_gram_op``: the cosine operator of one dataset (device pointers)."""
     _fields_ = [("n", _I64), ("m", _I64), ("indptr", _P), ("indices", _P), ("values", _P), ("colptr", _P),
                 ("rowidx", _P), ("cvalues", _P), ("w2", _P), ("a", _P), ("dinv", _P), ("w2_f32", _P),
-                ("a_f32", _P), ("dinv_f32", _P), ("staged_table_t", _P), ("staged_table_x", _P)]
+                ("a_f32", _P), ("dinv_f32", _P), ("staged_table_t", _P), ("staged_table_x", _P),
+                ("order_t", _P), ("order_t_positions", _I64)]
 
 
 class LanczosOpts(ctypes.Structure):
@@ -150,7 +155,7 @@ class LanczosInfo(ctypes.Structure):
 KERNELS_PER_CALL = {
     "sg_tile_plan": 4, "sg_tile_run": 5, "sg_tile_emit": 1, "sg_col_counts": 2, "sg_csr_select_cols": 5,
     "sg_csr_transpose": 8, "sg_spectral_prepare": 7, "sg_spmm": 1, "sg_spmm_ex": 1, "sg_spmm_masked": 1,
-    "sg_spmm_staged": 1, "sg_spmm_dyn": 1, "sg_spmm_ds": 1, "sg_ds_split": 1, "sg_idf_from_counts": 3, "sg_csr_row_norms": 1, "sg_staged_table": 1, "sg_gather_ceiling": 1, "sg_block_proj": 2, "sg_block_update": 1, "sg_block_cholqr": 4, "sg_block_finish": 1,
+    "sg_spmm_staged": 1, "sg_spmm_dyn": 1, "sg_spmm_ds": 1, "sg_ds_split": 1, "sg_spmm_dyn_ordered": 1, "sg_row_order": 10, "sg_idf_from_counts": 3, "sg_csr_row_norms": 1, "sg_staged_table": 1, "sg_gather_ceiling": 1, "sg_block_proj": 2, "sg_block_update": 1, "sg_block_cholqr": 4, "sg_block_finish": 1,
     "sg_lanczos_hblock": 1, "sg_basis_rotate": 1, "sg_fill_random": 1, "sg_knn": 6, "sg_knn_noalloc": 6,
     "sg_bblock_proj": 2, "sg_bblock_update": 1, "sg_bblock_cholqr": 4, "sg_blanczos_hblock": 1,
     "sg_bbasis_rotate": 1, "sg_bidf": 3, "sg_bmask": 1,

@@ -346,7 +346,10 @@ struct Apply {
     const void* yy = t ? nullptr : y;
     if (variant >= kDyn && code != 0) variant -= kDyn;  // the dynamic schedule is FP32 only
     int e;
-    if (variant >= kDyn) {
+    if (variant >= kDyn && t && op->order_t && op->order_t_positions > 0) {
+      e = sg_spmm_dyn_ordered(code, B, op->order_t_positions, ptr, idx, val, in, out, scale, dsh, yy,
+                              variant - kDyn, op->order_t, counter + which, s);
+    } else if (variant >= kDyn) {
       e = sg_spmm_dyn(code, B, rows, ptr, idx, val, in, out, scale, dsh, yy, variant - kDyn, nullptr,
                       counter + which, s);
     } else if (variant >= kStaged) {
@@ -586,10 +589,11 @@ extern "C" int sg_lanczos(const sg_gram_op* op, int precision, int block, int k,
     if (ds_sweep) {
       // Zs64 / T64 hold (hi, lo) FP32 pairs here: the same bytes as FP64
       SG_TRY(sg_ds_split(n, op->a, w.Up, w.Zs64, s));
-      SG_TRY(sg_spmm_ds(0, m, op->colptr, op->rowidx, op->cvalues, w.Zs64, w.T64, op->w2, nullptr, nullptr, rvt,
-                        w.counter, s));
+      const bool ordered = rvt >= 2 && op->order_t && op->order_t_positions > 0;
+      SG_TRY(sg_spmm_ds(0, ordered ? op->order_t_positions : m, op->colptr, op->rowidx, op->cvalues, w.Zs64, w.T64,
+                        op->w2, nullptr, nullptr, rvt, ordered ? op->order_t : nullptr, w.counter, s));
       SG_TRY(sg_spmm_ds(1, n, op->indptr, op->indices, op->values, w.T64, w.W64, op->a, op->dinv, w.Up, rvx,
-                        w.counter + 1, s));
+                        nullptr, w.counter + 1, s));
       nl += 3;
     } else {
       SG_TRY(sg_block_finish(1, kb, n, w.Up, nullptr, 0, 0, nullptr, w.Zs64, op->a, s));

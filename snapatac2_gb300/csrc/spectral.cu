@@ -327,13 +327,19 @@ __device__ __forceinline__ VT gather16(const VT* p, bool l2only) {
 // rows of a skewed matrix do not leave a tail of idle SMs; each row is still
 // summed by one warp in the same order (same result as the static schedule).
 constexpr int kDynRows = 4;
+// With `order` the counter walks positions instead of rows: order[p] is the
+// row at position p (-1: none), laid out by sg_row_order so that the longest
+// rows are taken first, one per 4-row fetch (longest-first scheduling: the
+// last rows to finish are short ones).  Each row is still summed by one warp
+// in the same order: the result does not change.
 
 template <typename T, int B, bool VALUED, bool SHIFT, int VAR, bool DYN = false>
 __global__ void __launch_bounds__(256)
 spmm_kernel(int64_t rows, const int64_t* __restrict__ ptr, const int32_t* __restrict__ idx,
             const float* __restrict__ val, const T* __restrict__ in, T* __restrict__ out,
             const T* __restrict__ scale, const T* __restrict__ dshift, const T* __restrict__ y,
-            const unsigned char* __restrict__ row_mask, unsigned int* __restrict__ counter = nullptr) {
+            const unsigned char* __restrict__ row_mask, unsigned int* __restrict__ counter = nullptr,
+            const int32_t* __restrict__ order = nullptr) {
   using VT = typename V16<T>::type;
   constexpr int VW = V16<T>::n;
   constexpr int LPN = B / VW;          // lanes per nonzero
@@ -360,8 +366,12 @@ spmm_kernel(int64_t rows, const int64_t* __restrict__ ptr, const int32_t* __rest
     } else if (r >= rows) {
       break;
     }
-    const int64_t rr = r;
+    int64_t rr = r;
     r += DYN ? 1 : nw;
+    if (DYN && order) {  // position -> row (-1: no row at this position)
+      rr = order[rr];
+      if (rr < 0) continue;
+    }
     if (row_mask && !row_mask[rr]) continue;  // frozen row (warp-uniform)
     const int64_t s = ptr[rr], e = ptr[rr + 1];
     VT acc = V16<T>::zero();
@@ -555,7 +565,7 @@ extern "C" int sg_spectral_prepare(int64_t n, int64_t m, const int64_t* indptr, 
 template <int B, int VAR>
 int launch_spmm_dyn_v(int64_t rows, const int64_t* ptr, const int32_t* idx, const float* val, const float* in,
                       float* out, const float* scale, const float* dshift, const float* y, cudaStream_t s,
-                      const unsigned char* mk, unsigned int* counter) {
+                      const unsigned char* mk, unsigned int* counter, const int32_t* order) {
   auto run = [&](auto kern) -> int {
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, 0) != cudaSuccess || per_sm < 1)
@@ -565,7 +575,7 @@ int launch_spmm_dyn_v(int64_t rows, const int64_t* ptr, const int32_t* idx, cons
     if (grid > need) grid = need;
     if (grid < 1) grid = 1;
     if (cudaMemsetAsync(counter, 0, sizeof(unsigned int), s) != cudaSuccess) return SG_ERR_CUDA;
-    kern<<<(unsigned)grid, 256, 0, s>>>(rows, ptr, idx, val, in, out, scale, dshift, y, mk, counter);
+    kern<<<(unsigned)grid, 256, 0, s>>>(rows, ptr, idx, val, in, out, scale, dshift, y, mk, counter, order);
     return cudaGetLastError() == cudaSuccess ? SG_OK : SG_ERR_CUDA;
   };
   if (val) {
@@ -579,16 +589,16 @@ int launch_spmm_dyn_v(int64_t rows, const int64_t* ptr, const int32_t* idx, cons
 template <int B>
 int launch_spmm_dyn_b(int variant, int64_t rows, const int64_t* ptr, const int32_t* idx, const float* val,
                       const float* in, float* out, const float* scale, const float* dshift, const float* y,
-                      cudaStream_t s, const unsigned char* mk, unsigned int* counter) {
+                      cudaStream_t s, const unsigned char* mk, unsigned int* counter, const int32_t* order) {
   switch (variant) {
-    case 0: return launch_spmm_dyn_v<B, 0>(rows, ptr, idx, val, in, out, scale, dshift, y, s, mk, counter);
-    case 1: return launch_spmm_dyn_v<B, 1>(rows, ptr, idx, val, in, out, scale, dshift, y, s, mk, counter);
-    case 2: return launch_spmm_dyn_v<B, 2>(rows, ptr, idx, val, in, out, scale, dshift, y, s, mk, counter);
-    case 3: return launch_spmm_dyn_v<B, 3>(rows, ptr, idx, val, in, out, scale, dshift, y, s, mk, counter);
-    case 4: return launch_spmm_dyn_v<B, 4>(rows, ptr, idx, val, in, out, scale, dshift, y, s, mk, counter);
-    case 5: return launch_spmm_dyn_v<B, 5>(rows, ptr, idx, val, in, out, scale, dshift, y, s, mk, counter);
-    case 6: return launch_spmm_dyn_v<B, 6>(rows, ptr, idx, val, in, out, scale, dshift, y, s, mk, counter);
-    case 7: return launch_spmm_dyn_v<B, 7>(rows, ptr, idx, val, in, out, scale, dshift, y, s, mk, counter);
+    case 0: return launch_spmm_dyn_v<B, 0>(rows, ptr, idx, val, in, out, scale, dshift, y, s, mk, counter, order);
+    case 1: return launch_spmm_dyn_v<B, 1>(rows, ptr, idx, val, in, out, scale, dshift, y, s, mk, counter, order);
+    case 2: return launch_spmm_dyn_v<B, 2>(rows, ptr, idx, val, in, out, scale, dshift, y, s, mk, counter, order);
+    case 3: return launch_spmm_dyn_v<B, 3>(rows, ptr, idx, val, in, out, scale, dshift, y, s, mk, counter, order);
+    case 4: return launch_spmm_dyn_v<B, 4>(rows, ptr, idx, val, in, out, scale, dshift, y, s, mk, counter, order);
+    case 5: return launch_spmm_dyn_v<B, 5>(rows, ptr, idx, val, in, out, scale, dshift, y, s, mk, counter, order);
+    case 6: return launch_spmm_dyn_v<B, 6>(rows, ptr, idx, val, in, out, scale, dshift, y, s, mk, counter, order);
+    case 7: return launch_spmm_dyn_v<B, 7>(rows, ptr, idx, val, in, out, scale, dshift, y, s, mk, counter, order);
     default: return SG_ERR_ARG;
   }
 }
@@ -653,10 +663,11 @@ extern "C" int sg_csr_row_norms(int64_t n, const int64_t* indptr, const int32_t*
 
 extern "C" int sg_spmm_variants(void) { return kSpmmVariants; }
 
-extern "C" int sg_spmm_dyn(int dtype, int block, int64_t rows, const int64_t* ptr, const int32_t* idx,
-                           const float* val, const void* in, void* out, const void* scale, const void* dshift,
-                           const void* y, int variant, const unsigned char* row_mask, unsigned int* counter,
-                           void* stream) {
+namespace sg {
+namespace {
+int spmm_dyn_impl(int dtype, int block, int64_t rows, const int64_t* ptr, const int32_t* idx, const float* val,
+                  const void* in, void* out, const void* scale, const void* dshift, const void* y, int variant,
+                  const int32_t* order, const unsigned char* row_mask, unsigned int* counter, void* stream) {
   if (rows < 0 || rows >= (int64_t(1) << 31) || !scale || (dshift && !y) || !counter || variant < 0 ||
       variant >= kSpmmVariants || dtype != 0)
     return SG_ERR_ARG;
@@ -665,12 +676,101 @@ extern "C" int sg_spmm_dyn(int dtype, int block, int64_t rows, const int64_t* pt
   const float *fi = (const float*)in, *fs = (const float*)scale, *fd = (const float*)dshift, *fy = (const float*)y;
   float* fo = (float*)out;
   switch (block) {
-    case 4: return launch_spmm_dyn_b<4>(variant, rows, ptr, idx, val, fi, fo, fs, fd, fy, s, row_mask, counter);
-    case 8: return launch_spmm_dyn_b<8>(variant, rows, ptr, idx, val, fi, fo, fs, fd, fy, s, row_mask, counter);
-    case 16: return launch_spmm_dyn_b<16>(variant, rows, ptr, idx, val, fi, fo, fs, fd, fy, s, row_mask, counter);
-    case 32: return launch_spmm_dyn_b<32>(variant, rows, ptr, idx, val, fi, fo, fs, fd, fy, s, row_mask, counter);
+    case 4: return launch_spmm_dyn_b<4>(variant, rows, ptr, idx, val, fi, fo, fs, fd, fy, s, row_mask, counter, order);
+    case 8: return launch_spmm_dyn_b<8>(variant, rows, ptr, idx, val, fi, fo, fs, fd, fy, s, row_mask, counter, order);
+    case 16:
+      return launch_spmm_dyn_b<16>(variant, rows, ptr, idx, val, fi, fo, fs, fd, fy, s, row_mask, counter, order);
+    case 32:
+      return launch_spmm_dyn_b<32>(variant, rows, ptr, idx, val, fi, fo, fs, fd, fy, s, row_mask, counter, order);
     default: return SG_ERR_ARG;
   }
+}
+
+// keys: ~len (descending length under an ascending sort), values: row index
+__global__ void order_keys_kernel(int64_t rows, const int64_t* __restrict__ ptr, uint64_t* __restrict__ keys,
+                                  uint64_t* __restrict__ vals) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < rows; r += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t len = ptr[r + 1] - ptr[r];
+    keys[r] = 0xffffffffull - (uint64_t)(len < 0xffffffffll ? len : 0xffffffffll);
+    vals[r] = (uint64_t)r;
+  }
+}
+
+// position p = 4c + j holds the row of sorted rank c + j·C (C = ceil(rows/4)):
+// each 4-row fetch gets one row of every quarter of the length order
+__global__ void order_deal_kernel(int64_t rows, int64_t C, const uint64_t* __restrict__ sorted_rows,
+                                  int32_t* __restrict__ order) {
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < 4 * C; p += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t c = p >> 2, j = p & 3;
+    const int64_t q = c + j * C;
+    order[p] = q < rows ? (int32_t)sorted_rows[q] : -1;
+  }
+}
+
+struct OrderLayout {
+  uint64_t *keys, *vals, *keys_alt, *vals_alt;
+  void* radix;
+  int64_t bytes;
+};
+
+OrderLayout order_layout(char* base, int64_t rows) {
+  OrderLayout L{};
+  int64_t o = 0;
+  auto take = [&](int64_t b) { const int64_t r = o; o += (b + 255) / 256 * 256; return r; };
+  const int64_t R = rows > 0 ? rows : 1;
+  const int64_t ok = take(8 * R), ov = take(8 * R), oka = take(8 * R), ova = take(8 * R), orad = take(radix_scratch_bytes(R));
+  if (base) {
+    L.keys = (uint64_t*)(base + ok);
+    L.vals = (uint64_t*)(base + ov);
+    L.keys_alt = (uint64_t*)(base + oka);
+    L.vals_alt = (uint64_t*)(base + ova);
+    L.radix = base + orad;
+  }
+  L.bytes = o;
+  return L;
+}
+}  // namespace
+}  // namespace sg
+
+extern "C" int sg_spmm_dyn(int dtype, int block, int64_t rows, const int64_t* ptr, const int32_t* idx,
+                           const float* val, const void* in, void* out, const void* scale, const void* dshift,
+                           const void* y, int variant, const unsigned char* row_mask, unsigned int* counter,
+                           void* stream) {
+  return spmm_dyn_impl(dtype, block, rows, ptr, idx, val, in, out, scale, dshift, y, variant, nullptr, row_mask,
+                       counter, stream);
+}
+
+extern "C" int sg_spmm_dyn_ordered(int dtype, int block, int64_t positions, const int64_t* ptr, const int32_t* idx,
+                                   const float* val, const void* in, void* out, const void* scale,
+                                   const void* dshift, const void* y, int variant, const int32_t* order,
+                                   unsigned int* counter, void* stream) {
+  if (!order) return SG_ERR_ARG;
+  return spmm_dyn_impl(dtype, block, positions, ptr, idx, val, in, out, scale, dshift, y, variant, order, nullptr,
+                       counter, stream);
+}
+
+extern "C" int64_t sg_row_order_positions(int64_t rows) { return rows < 0 ? -1 : 4 * ((rows + 3) / 4); }
+
+extern "C" int64_t sg_row_order_scratch_bytes(int64_t rows) { return rows < 0 ? -1 : order_layout(nullptr, rows).bytes; }
+
+extern "C" int sg_row_order(int64_t rows, const int64_t* ptr, int32_t* order, void* scratch, int64_t scratch_bytes,
+                            void* stream) {
+  if (rows < 0 || rows >= (int64_t(1) << 31) || (rows > 0 && (!ptr || !order || !scratch))) return SG_ERR_ARG;
+  if (((uintptr_t)scratch & 255u) != 0) return SG_ERR_ARG;
+  if (rows == 0) return SG_OK;
+  OrderLayout L = order_layout((char*)scratch, rows);
+  if (scratch_bytes < L.bytes) return SG_ERR_CAP;
+  cudaStream_t s = as_stream(stream);
+  const int g = grid_for(rows, 256, 16 * sm_count());
+  order_keys_kernel<<<g, 256, 0, s>>>(rows, ptr, L.keys, L.vals);
+  SG_CHECK_LAUNCH();
+  bool alt = false;
+  if (radix_sort_u64(rows, L.keys, L.vals, L.keys_alt, L.vals_alt, 0, 32, L.radix, s, &alt) != cudaSuccess)
+    return SG_ERR_CUDA;
+  const int64_t C = (rows + 3) / 4;
+  order_deal_kernel<<<grid_for(4 * C, 256, 16 * sm_count()), 256, 0, s>>>(rows, C, alt ? L.vals_alt : L.vals, order);
+  SG_CHECK_LAUNCH();
+  return SG_OK;
 }
 
 extern "C" int sg_spmm_masked(int dtype, int block, int64_t rows, const int64_t* ptr, const int32_t* idx,

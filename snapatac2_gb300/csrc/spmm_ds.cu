@@ -42,7 +42,7 @@ __global__ void __launch_bounds__(256)
 spmm_ds_kernel(int64_t rows, const int64_t* __restrict__ ptr, const int32_t* __restrict__ idx,
                const float* __restrict__ val, const float4* __restrict__ in, void* __restrict__ out,
                const double* __restrict__ scale, const double* __restrict__ dshift, const double* __restrict__ y,
-               unsigned int* __restrict__ counter) {
+               unsigned int* __restrict__ counter, const int32_t* __restrict__ order) {
   constexpr int LPN = kDsVec, NPS = 32 / LPN;
   const int lane = threadIdx.x & 31;
   const int sub = lane % LPN, slot = lane / LPN;
@@ -62,8 +62,12 @@ spmm_ds_kernel(int64_t rows, const int64_t* __restrict__ ptr, const int32_t* __r
     } else if (r >= rows) {
       break;
     }
-    const int64_t rr = r;
+    int64_t rr = r;
     r += DYN ? 1 : nw;
+    if (DYN && order) {  // position -> row (-1: none), longest rows first
+      rr = order[rr];
+      if (rr < 0) continue;
+    }
     const int64_t s = ptr[rr], e = ptr[rr + 1];
     float s0 = 0.f, c0 = 0.f, s1 = 0.f, c1 = 0.f;
     for (int64_t base = s; base < e; base += 32 * CH) {
@@ -158,7 +162,8 @@ int sm_count_ds() {
 
 template <bool VALUED, bool XPASS, int CH, bool DYN>
 int launch_ds(int64_t rows, const int64_t* ptr, const int32_t* idx, const float* val, const void* in, void* out,
-              const double* scale, const double* dshift, const double* y, unsigned int* counter, cudaStream_t s) {
+              const double* scale, const double* dshift, const double* y, unsigned int* counter,
+              const int32_t* order, cudaStream_t s) {
   auto kern = spmm_ds_kernel<VALUED, XPASS, CH, DYN>;
   int64_t grid;
   if (DYN) {
@@ -174,19 +179,19 @@ int launch_ds(int64_t rows, const int64_t* ptr, const int32_t* idx, const float*
     grid = grid_for(rows * 32, 256, 32 * sm_count_ds());
   }
   kern<<<(unsigned)grid, 256, 0, s>>>(rows, ptr, idx, val, static_cast<const float4*>(in), out, scale, dshift, y,
-                                      counter);
+                                      counter, order);
   return cudaGetLastError() == cudaSuccess ? SG_OK : SG_ERR_CUDA;
 }
 
 template <bool VALUED, bool XPASS>
 int launch_ds_v(int variant, int64_t rows, const int64_t* ptr, const int32_t* idx, const float* val, const void* in,
                 void* out, const double* scale, const double* dshift, const double* y, unsigned int* counter,
-                cudaStream_t s) {
+                const int32_t* order, cudaStream_t s) {
   switch (variant) {
-    case 0: return launch_ds<VALUED, XPASS, 1, false>(rows, ptr, idx, val, in, out, scale, dshift, y, counter, s);
-    case 1: return launch_ds<VALUED, XPASS, 2, false>(rows, ptr, idx, val, in, out, scale, dshift, y, counter, s);
-    case 2: return launch_ds<VALUED, XPASS, 1, true>(rows, ptr, idx, val, in, out, scale, dshift, y, counter, s);
-    case 3: return launch_ds<VALUED, XPASS, 2, true>(rows, ptr, idx, val, in, out, scale, dshift, y, counter, s);
+    case 0: return launch_ds<VALUED, XPASS, 1, false>(rows, ptr, idx, val, in, out, scale, dshift, y, counter, nullptr, s);
+    case 1: return launch_ds<VALUED, XPASS, 2, false>(rows, ptr, idx, val, in, out, scale, dshift, y, counter, nullptr, s);
+    case 2: return launch_ds<VALUED, XPASS, 1, true>(rows, ptr, idx, val, in, out, scale, dshift, y, counter, order, s);
+    case 3: return launch_ds<VALUED, XPASS, 2, true>(rows, ptr, idx, val, in, out, scale, dshift, y, counter, order, s);
     default: return SG_ERR_ARG;
   }
 }
@@ -200,21 +205,21 @@ extern "C" int sg_spmm_ds_variants(void) { return 4; }
 
 extern "C" int sg_spmm_ds(int pass, int64_t rows, const int64_t* ptr, const int32_t* idx, const float* val,
                           const void* in, void* out, const double* scale, const double* dshift, const double* y,
-                          int variant, unsigned int* counter, void* stream) {
+                          int variant, const int32_t* order, unsigned int* counter, void* stream) {
   if ((pass != 0 && pass != 1) || rows < 0 || rows >= (int64_t(1) << 31) || variant < 0 || variant > 3 ||
       (rows > 0 && (!ptr || !idx || !in || !out || !scale)) || (dshift && (!y || pass == 0)) ||
-      (variant >= 2 && !counter))
+      (variant >= 2 && !counter) || (order && variant < 2))
     return SG_ERR_ARG;
   if (((uintptr_t)in & 15u) != 0 || ((uintptr_t)out & 15u) != 0 || (y && ((uintptr_t)y & 15u) != 0))
     return SG_ERR_ARG;
   if (rows == 0) return SG_OK;
   cudaStream_t s = as_stream(stream);
   if (val) {
-    if (pass) return launch_ds_v<true, true>(variant, rows, ptr, idx, val, in, out, scale, dshift, y, counter, s);
-    return launch_ds_v<true, false>(variant, rows, ptr, idx, val, in, out, scale, dshift, y, counter, s);
+    if (pass) return launch_ds_v<true, true>(variant, rows, ptr, idx, val, in, out, scale, dshift, y, counter, order, s);
+    return launch_ds_v<true, false>(variant, rows, ptr, idx, val, in, out, scale, dshift, y, counter, order, s);
   }
-  if (pass) return launch_ds_v<false, true>(variant, rows, ptr, idx, val, in, out, scale, dshift, y, counter, s);
-  return launch_ds_v<false, false>(variant, rows, ptr, idx, val, in, out, scale, dshift, y, counter, s);
+  if (pass) return launch_ds_v<false, true>(variant, rows, ptr, idx, val, in, out, scale, dshift, y, counter, order, s);
+  return launch_ds_v<false, false>(variant, rows, ptr, idx, val, in, out, scale, dshift, y, counter, order, s);
 }
 
 extern "C" int sg_ds_split(int64_t n, const double* a, const double* U, void* out, void* stream) {

@@ -30,13 +30,14 @@ def _dev(x):
     return torch.from_numpy(np.ascontiguousarray(x)).cuda() if x is not None else None
 
 
-def _run(L, pass_, rows, ip, ix, vl, pairs, scale, dshift=None, y=None, variant=0):
+def _run(L, pass_, rows, ip, ix, vl, pairs, scale, dshift=None, y=None, variant=0, order=None):
     import torch
     out = torch.empty(rows, 32, dtype=torch.float64, device="cuda")  # pairs: same bytes
     cnt = torch.zeros(1, dtype=torch.int32, device="cuda")
     p = lambda t: t.data_ptr() if t is not None else None  # noqa: E731
-    rc = L.sg_spmm_ds(pass_, rows, p(ip), p(ix), p(vl), pairs.data_ptr(), out.data_ptr(), p(scale), p(dshift), p(y),
-                      variant, cnt.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    npos = order.numel() if order is not None else rows
+    rc = L.sg_spmm_ds(pass_, npos, p(ip), p(ix), p(vl), pairs.data_ptr(), out.data_ptr(), p(scale), p(dshift), p(y),
+                      variant, p(order), cnt.data_ptr(), torch.cuda.current_stream().cuda_stream)
     torch.cuda.synchronize()
     assert rc == 0
     return out
@@ -79,6 +80,20 @@ def test_compensated_sums_are_fp64_class(valued):
     assert np.all(err <= tol), float((err / np.maximum(absum, 1e-300)).max())
     for o in outs[1:]:  # every variant: same order of operations, same bits
         assert torch.equal(o, outs[0])
+    # longest rows first (sg_row_order): same bits again
+    npos = int(L.sg_row_order_positions(rows))
+    order = torch.empty(npos, dtype=torch.int32, device="cuda")
+    nb = int(L.sg_row_order_scratch_bytes(rows))
+    scr = torch.empty(nb, dtype=torch.uint8, device="cuda")
+    assert L.sg_row_order(rows, d_ip.data_ptr(), order.data_ptr(), scr.data_ptr(), nb, 0) == 0
+    for vv in (2, 3):
+        o = torch.empty_like(outs[0])
+        cnt = torch.zeros(1, dtype=torch.int32, device="cuda")
+        assert L.sg_spmm_ds(0, npos, d_ip.data_ptr(), d_ix.data_ptr(), d_vl.data_ptr() if d_vl is not None else None,
+                            pairs.data_ptr(), o.data_ptr(), d_s.data_ptr(), None, None, vv, order.data_ptr(),
+                            cnt.data_ptr(), 0) == 0
+        torch.cuda.synchronize()
+        assert torch.equal(o, outs[0])
     assert torch.equal(_run(L, 0, rows, d_ip, d_ix, d_vl, pairs, d_s, variant=3), outs[0])
     # pass 1 (FP64 out with the shift) against the FP64 gather kernel
     T = outs[0]
@@ -114,10 +129,11 @@ def test_spmm_ds_refuses_bad_arguments():
     buf = torch.zeros(64, dtype=torch.float64, device="cuda")
     ip = torch.zeros(2, dtype=torch.int64, device="cuda")
     p = buf.data_ptr()
-    assert L.sg_spmm_ds(2, 1, ip.data_ptr(), p, None, p, p, p, None, None, 0, None, 0) == _lib.SG_ERR_ARG
-    assert L.sg_spmm_ds(0, 1, ip.data_ptr(), p, None, p, p, p, p, p, 0, None, 0) == _lib.SG_ERR_ARG  # shift in pass 0
-    assert L.sg_spmm_ds(0, 1, ip.data_ptr(), p, None, p, p, p, None, None, 2, None, 0) == _lib.SG_ERR_ARG  # no counter
-    assert L.sg_spmm_ds(0, 1, ip.data_ptr(), p, None, p + 8, p, p, None, None, 0, None, 0) == _lib.SG_ERR_ARG  # misaligned
+    assert L.sg_spmm_ds(2, 1, ip.data_ptr(), p, None, p, p, p, None, None, 0, None, None, 0) == _lib.SG_ERR_ARG
+    assert L.sg_spmm_ds(0, 1, ip.data_ptr(), p, None, p, p, p, p, p, 0, None, None, 0) == _lib.SG_ERR_ARG  # shift in pass 0
+    assert L.sg_spmm_ds(0, 1, ip.data_ptr(), p, None, p, p, p, None, None, 2, None, None, 0) == _lib.SG_ERR_ARG  # no counter
+    assert L.sg_spmm_ds(0, 1, ip.data_ptr(), p, None, p + 8, p, p, None, None, 0, None, None, 0) == _lib.SG_ERR_ARG  # misaligned
+    assert L.sg_spmm_ds(0, 4, ip.data_ptr(), p, None, p, p, p, None, None, 1, ip.data_ptr(), None, 0) == _lib.SG_ERR_ARG  # order, static
     assert L.sg_spmm_ds_variants() == 4
 
 

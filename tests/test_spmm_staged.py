@@ -176,6 +176,23 @@ def test_dynamic_schedule_equals_static(block, valued, shift, masked, variant):
     assert torch.equal(o1, o2)
     assert L.sg_spmm_dyn(1, block, rows, ip.data_ptr(), ix.data_ptr(), None, inp.data_ptr(), o2.data_ptr(),
                          sc.data_ptr(), None, None, 0, None, cnt.data_ptr(), sh) == _lib.SG_ERR_ARG
+    if not masked:
+        # longest rows first (sg_row_order): every row once, same bits
+        npos = int(L.sg_row_order_positions(rows))
+        order = torch.empty(npos, dtype=torch.int32, device=dev)
+        nb = int(L.sg_row_order_scratch_bytes(rows))
+        scr = torch.empty(nb, dtype=torch.uint8, device=dev)
+        _lib.check(L.sg_row_order(rows, ip.data_ptr(), order.data_ptr(), scr.data_ptr(), nb, sh), "order")
+        o3 = torch.full((rows, block), 7.0, dtype=torch.float32, device=dev)
+        _lib.check(L.sg_spmm_dyn_ordered(0, block, npos, ip.data_ptr(), ix.data_ptr(), p(val), inp.data_ptr(),
+                                         o3.data_ptr(), sc.data_ptr(), p(dsh), p(y), variant, order.data_ptr(),
+                                         cnt.data_ptr(), sh), "ordered")
+        torch.cuda.synchronize()
+        assert torch.equal(o1, o3)
+        oh = order.cpu().numpy()
+        assert np.array_equal(np.sort(oh[oh >= 0]), np.arange(rows))  # a permutation of the rows
+        first = oh[0::4][: rows // 8]                                  # the first row of each fetch
+        assert np.all(np.diff(np.diff(indptr)[first]) <= 0)           # by descending length
 
 
 @pytest.mark.gpu
