@@ -230,10 +230,11 @@ update_kernel(int64_t n, const T* __restrict__ Q, int64_t ldq, int ncols, const 
 }
 
 // ---- FP32 tiled forms of proj and update -----------------------------------
-// The basis is read in stages of 32 columns (128 bytes of a row) by
+// The basis is read in stages of 32 columns (128 bytes of a row; 16 in the
+// update, whose smaller rings let three CTAs share an SM) by
 // cp.async into per-warp shared-memory rings; rows of a staged tile are
-// padded to 36 floats, so the 16-byte reads of eight consecutive rows touch
-// 32 distinct banks.  Columns past ncols and rows past the limit are
+// padded by 4 floats (36 or 20), so the 16-byte reads of eight consecutive
+// rows touch 32 distinct banks.  Columns past ncols and rows past the limit are
 // zero-filled by the copy itself (src-size < 16), so the inner loops have no
 // bounds tests.  Only used when Q, W and every row start are 16-byte aligned.
 constexpr int kStageCols = 32;
@@ -250,23 +251,30 @@ __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
-// rows [row0, row0 + R) x columns [col0, col0 + 32) of Q into buf (R x kPitch);
-// rows at or past rlim and columns at or past ncols read as zero
-template <int R>
+// rows [row0, row0 + R) x columns [col0, col0 + SC) of Q into buf (R rows of
+// SC + 4 floats); rows at or past rlim and columns at or past ncols read as
+// zero.  Rows of SC + 4 floats (SC = 16 or 32) put the 16-byte reads of eight
+// consecutive rows on 32 distinct banks.
+template <int R, int SC = kStageCols>
 __device__ __forceinline__ void stage_q(float* buf, const float* __restrict__ Q, int64_t ldq, int64_t rlim,
                                         int ncols, int64_t row0, int col0, int lane) {
+  constexpr int CPR = SC / 4;  // 16-byte chunks per row
 #pragma unroll
-  for (int j = 0; j < R / 4; ++j) {
+  for (int j = 0; j < R * CPR / 32; ++j) {
     const int idx = j * 32 + lane;
-    const int r = idx >> 3, c = (idx & 7) * 4;
+    const int r = idx / CPR, c = (idx % CPR) * 4;
     const int64_t row = row0 + r;
     const int col = col0 + c;
     int bytes = (ncols - col) * 4;
     bytes = bytes < 0 ? 0 : (bytes > 16 ? 16 : bytes);
     if (row >= rlim) bytes = 0;
-    cp_async16(buf + r * kPitch + c, bytes ? Q + row * ldq + col : Q, bytes);
+    cp_async16(buf + r * (SC + 4) + c, bytes ? Q + row * ldq + col : Q, bytes);
   }
 }
+
+// basis columns per stage of the update: 16 (smaller rings, three CTAs per SM)
+constexpr int kUpdCols = 16;
+constexpr int kUpdPitch = kUpdCols + 4;
 
 // W -= Q[:, :ncols] C.  Each warp owns 64-row tiles (rows lane and lane + 32
 // of a tile per lane, all B columns in registers); C (FP32, zero past ncols)
@@ -279,19 +287,19 @@ update_tiled(int64_t n, const float* __restrict__ Q, int64_t ldq, int ncols, con
              float* __restrict__ W) {
   constexpr int R = 64;
   extern __shared__ __align__(16) unsigned char sraw[];
-  const int nch = (ncols + kStageCols - 1) / kStageCols;
+  const int nch = (ncols + kUpdCols - 1) / kUpdCols;
   float* cs = reinterpret_cast<float*>(sraw);
-  float* ring = cs + (size_t)nch * kStageCols * B;
-  for (int t = threadIdx.x; t < nch * kStageCols * B; t += blockDim.x) cs[t] = t < ncols * B ? (float)C[t] : 0.f;
+  float* ring = cs + (size_t)nch * kUpdCols * B;
+  for (int t = threadIdx.x; t < nch * kUpdCols * B; t += blockDim.x) cs[t] = t < ncols * B ? (float)C[t] : 0.f;
   __syncthreads();
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  float* buf = ring + (size_t)wid * 2 * R * kPitch;
+  float* buf = ring + (size_t)wid * 2 * R * kUpdPitch;
   const int64_t ntiles = (n + R - 1) / R;
   const int64_t nw = (int64_t)gridDim.x * kTileWarps;
   int64_t tile = blockIdx.x * (int64_t)kTileWarps + wid;
   if (tile >= ntiles) return;
   int ch = 0, sl = 0;
-  stage_q<R>(buf, Q, ldq, n, ncols, tile * R, 0, lane);
+  stage_q<R, kUpdCols>(buf, Q, ldq, n, ncols, tile * R, 0, lane);
   cp_async_commit();
   float a0[B], a1[B];
 #pragma unroll
@@ -304,16 +312,16 @@ update_tiled(int64_t n, const float* __restrict__ Q, int64_t ldq, int ncols, con
       ntile = tile + nw;
     }
     const bool more = ntile < ntiles;
-    if (more) stage_q<R>(buf + (sl ^ 1) * R * kPitch, Q, ldq, n, ncols, ntile * R, nchk * kStageCols, lane);
+    if (more) stage_q<R, kUpdCols>(buf + (sl ^ 1) * R * kUpdPitch, Q, ldq, n, ncols, ntile * R, nchk * kUpdCols, lane);
     cp_async_commit();
     cp_async_wait<1>();
     __syncwarp();
-    const float* qb = buf + sl * R * kPitch;
-    const float* cst = cs + (size_t)ch * kStageCols * B;
+    const float* qb = buf + sl * R * kUpdPitch;
+    const float* cst = cs + (size_t)ch * kUpdCols * B;
 #pragma unroll 2
-    for (int p4 = 0; p4 < kStageCols / 4; ++p4) {
-      const float4 qa = *reinterpret_cast<const float4*>(qb + lane * kPitch + 4 * p4);
-      const float4 qc = *reinterpret_cast<const float4*>(qb + (lane + 32) * kPitch + 4 * p4);
+    for (int p4 = 0; p4 < kUpdCols / 4; ++p4) {
+      const float4 qa = *reinterpret_cast<const float4*>(qb + lane * kUpdPitch + 4 * p4);
+      const float4 qc = *reinterpret_cast<const float4*>(qb + (lane + 32) * kUpdPitch + 4 * p4);
       const float va[4] = {qa.x, qa.y, qa.z, qa.w}, vc[4] = {qc.x, qc.y, qc.z, qc.w};
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
@@ -473,8 +481,8 @@ proj_tiled(int64_t n, const float* __restrict__ Q, int64_t ldq, int ncols, const
 }
 
 size_t update_tiled_smem(int B, int ncols) {
-  const int nch = (ncols + kStageCols - 1) / kStageCols;
-  return (size_t)nch * kStageCols * B * 4 + (size_t)kTileWarps * 2 * 64 * kPitch * 4;
+  const int nch = (ncols + kUpdCols - 1) / kUpdCols;
+  return (size_t)nch * kUpdCols * B * 4 + (size_t)kTileWarps * 2 * 64 * kUpdPitch * 4;
 }
 
 template <int B>
