@@ -14,8 +14,6 @@
 //   finish  Q[:, col:col+B] = W, Z = W, Zs = a ⊙ W
 //   hblock  Rayleigh-quotient diagonal block and coupling R into H (FP64)
 //   rotate  out = Q[:, :m] Y                (thick restart, Ritz vectors)
-#include <mutex>
-
 #include "common.cuh"
 #include "internal.h"
 
@@ -720,12 +718,11 @@ template <int B>
 int proj_tiled_launch(int64_t n, const float* Q, int64_t ldq, int ncols, const float* W, double* part, int nparts,
                       double* C, cudaStream_t s) {
   const size_t smem = proj_tiled_smem<B>();
-  static std::once_flag once;
-  static cudaError_t attr = cudaSuccess;
-  std::call_once(once, [&] {
-    attr = cudaFuncSetAttribute(proj_tiled<B>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTiledSmemCap);
-  });
-  if (attr != cudaSuccess) return SG_ERR_CUDA;
+  // set on every call (the attribute is per device); always the same fixed
+  // cap, so concurrent callers cannot lower it under one another
+  if (cudaFuncSetAttribute(proj_tiled<B>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTiledSmemCap) !=
+      cudaSuccess)
+    return SG_ERR_CUDA;
   proj_tiled<B><<<nparts, kTileWarps * 32, smem, s>>>(n, Q, ldq, ncols, W, part);
   SG_CHECK_LAUNCH();
   proj_reduce<<<(ncols * B + 31) / 32, kReduceWarps * 32, 0, s>>>(nparts, ncols, B, part, C);
@@ -776,12 +773,9 @@ int update_tiled_launch(int64_t n, const float* Q, int64_t ldq, int ncols, const
                         cudaStream_t s) {
   const size_t smem = update_tiled_smem(B, ncols);
   if (smem > (size_t)kTiledSmemCap) return SG_ERR_ARG;
-  static std::once_flag once;
-  static cudaError_t attr = cudaSuccess;
-  std::call_once(once, [&] {
-    attr = cudaFuncSetAttribute(update_tiled<B>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTiledSmemCap);
-  });
-  if (attr != cudaSuccess) return SG_ERR_CUDA;
+  if (cudaFuncSetAttribute(update_tiled<B>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTiledSmemCap) !=
+      cudaSuccess)
+    return SG_ERR_CUDA;
   int occ = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, update_tiled<B>, kTileWarps * 32, smem) != cudaSuccess)
     return SG_ERR_CUDA;
