@@ -10,7 +10,14 @@ Python for the spectral path, run on small seeded inputs:
                    chunk of cells, eigenvectors and eigenvalues with a
                    negative entry (so some d <= 0 are replaced);
 * ``orthogonalize`` (snapatac2-python/python/snapatac2/tools/_embedding.py:397-413)
-                   on a seeded n x k matrix and eigenvalues.
+                   on a seeded n x k matrix and eigenvalues;
+* ``SpectralMatrixFree.fit`` (_embedding.py:434-465, the Python twin of the
+                   Rust ``spectral_mf`` normalisation and degree of
+                   embedding.rs:133-152, 315-326) with the class's ``_eigen``
+                   (_embedding.py:475-481), on the 300-cell matrix (binary and
+                   with counts) and seeded feature weights: the normalised,
+                   degree-scaled matrix and 1/D handed to ``_eigen`` are
+                   captured, and the eigenvalues kept.
 
 The strings are cut out of the Rust source and the function out of the
 Python source (``ast``), then executed with NumPy / SciPy only.  Inputs
@@ -48,11 +55,44 @@ def embedded(name: str):
     return ns[name]
 
 
-def python_function(name: str):
+def python_function(name: str, ns: dict | None = None):
     fn = next(n for n in ast.parse(open(REF_PY).read()).body if isinstance(n, ast.FunctionDef) and n.name == name)
-    ns = {"np": np}
+    ns = {"np": np} if ns is None else ns
     exec(compile(ast.Module(body=[fn], type_ignores=[]), REF_PY, "exec"), ns)
     return ns[name]
+
+
+def python_class(name: str, ns: dict):
+    cls = next(n for n in ast.parse(open(REF_PY).read()).body if isinstance(n, ast.ClassDef) and n.name == name)
+    exec(compile(ast.Module(body=[cls], type_ignores=[]), REF_PY, "exec"), ns)
+    return ns[name]
+
+
+def spectral_mf_inputs(valued: bool):
+    from snapatac2_gb300 import synthetic as S
+    B = S.binary_csr(300, 2000, nnz_per_cell=60, seed=5)
+    vals = np.random.default_rng(7).integers(1, 4, B.nnz).astype(np.float64) if valued else np.ones(B.nnz)
+    X = sp.csr_matrix((vals, B.indices, B.indptr), shape=B.shape)
+    w = np.random.default_rng(6).uniform(0.5, 3.0, B.shape[1])
+    return X, w
+
+
+def spectral_mf(X, w):
+    import logging
+    import scipy
+    import scipy.sparse.linalg  # noqa: F401
+    eig = python_function("_eigen", {"np": np, "sp": scipy})
+    captured = {}
+
+    def capture(Xs, dinv, k):
+        captured["X"], captured["dinv"] = sp.csr_matrix(Xs), np.asarray(dinv)
+        return eig(Xs, dinv, k)
+
+    cls = python_class("SpectralMatrixFree", {"np": np, "sp": scipy, "_eigen": capture, "logging": logging})
+    model = cls(out_dim=8, feature_weights=w).fit(X, verbose=0)
+    Xs = captured["X"]
+    Xs.sort_indices()
+    return Xs, captured["dinv"], np.real(model.evals)
 
 
 def eigen_inputs():
@@ -91,6 +131,11 @@ def main() -> None:
     evals, q = orthogonalize_inputs()
     e, V = python_function("orthogonalize")(evals, q)
     out["orth_evals"], out["orth_evecs"] = np.real(e), np.real(V)
+    for tag, valued in (("mf", False), ("mfv", True)):
+        X, w = spectral_mf_inputs(valued)
+        Xs, dinv, ev = spectral_mf(X, w)
+        out[f"{tag}_xs_data"], out[f"{tag}_xs_indices"], out[f"{tag}_xs_indptr"] = Xs.data, Xs.indices, Xs.indptr
+        out[f"{tag}_dinv"], out[f"{tag}_evals"] = dinv, ev
     np.savez_compressed(os.path.join(ROOT, "tests", "golden", "embedding.npz"), **out)
 
 

@@ -1,8 +1,10 @@
 """The oracle's spectral steps and the package's orthogonalisation against
 golden outputs of the reference's own Python (CPU): the ``eigen`` and
 ``nystrom`` functions embedded in snapatac2-python/src/embedding.rs:158-171
-and 222-229, and ``orthogonalize`` (tools/_embedding.py:397-413), run on
-seeded inputs by ``tests/golden/make_embedding_golden.py``."""
+and 222-229, ``orthogonalize`` (tools/_embedding.py:397-413), and the
+normalisation and degree scaling of ``SpectralMatrixFree.fit``
+(tools/_embedding.py:447-458, the Python twin of embedding.rs:133-152,
+315-326), run on seeded inputs by ``tests/golden/make_embedding_golden.py``."""
 import importlib.util
 import os
 
@@ -33,6 +35,25 @@ def test_oracle_eigen_is_the_reference_call():
     ev, U = osp.eigen(Xs, dinv, 8, 0)
     np.testing.assert_allclose(ev, GOLDEN["eigen_evals"], rtol=1e-12)
     _cols_match(U, GOLDEN["eigen_evecs"], 1e-8)
+
+
+@pytest.mark.parametrize("tag,valued", [("mf", False), ("mfv", True)])
+def test_oracle_normalize_and_degree_are_the_reference_python(tag, valued):
+    """Rows scaled by 1 / ||x_i ⊙ w|| after the feature weights, the degree
+    d = X (Xᵀ 1) - 1 and the rows scaled by d^-1/2: the matrix and 1/d that
+    the reference's Python hands to ``_eigen``, for given weights (binary
+    matrix and counts); and the eigenvalues of that operator."""
+    import scipy.sparse as sp
+    X, w = gen.spectral_mf_inputs(valued)
+    Xs, dinv = osp.degree_scale(osp.normalize(X, w))
+    Xs = sp.csr_matrix(Xs)
+    Xs.sort_indices()
+    np.testing.assert_allclose(dinv, GOLDEN[f"{tag}_dinv"], rtol=1e-13)
+    assert np.array_equal(Xs.indptr, GOLDEN[f"{tag}_xs_indptr"])
+    assert np.array_equal(Xs.indices, GOLDEN[f"{tag}_xs_indices"])
+    np.testing.assert_allclose(Xs.data, GOLDEN[f"{tag}_xs_data"], rtol=1e-13)
+    ev, _ = osp.eigen(Xs, dinv, 8, 0)
+    np.testing.assert_allclose(np.sort(ev)[::-1], GOLDEN[f"{tag}_evals"], rtol=1e-10)
 
 
 def test_oracle_nystrom_chunk_is_the_reference_function():
