@@ -14,6 +14,12 @@ FP64 restatement of the reference's matrix-free cosine spectral embedding:
                    (``gram.c``) for sizes where SciPy's would take minutes.
 * ``spectral``     ``snapatac2-python/python/snapatac2/tools/_embedding.py:223-293``
                    (n_comps clamp, ``weighted_by_sd`` filter and scaling).
+
+Pinned: ``eigen`` by golden outputs of the reference's embedded string;
+``normalize`` and ``degree_scale`` by golden outputs of the reference's own
+Python twin ``SpectralMatrixFree.fit`` (tools/_embedding.py:447-458), both
+made by ``tests/golden/make_embedding_golden.py``.  ``idf`` has no reference
+test or Python twin: parity unpinned for that formula.
 """
 from __future__ import annotations
 
